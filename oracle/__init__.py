@@ -1,0 +1,533 @@
+"""CPU oracle for the ESPERANTO read-alignment inner loop (TEST INFRASTRUCTURE).
+
+This package wraps the C restatement in this directory (extend.c, myers.c,
+split.c, batch.c) with ctypes.  Only the test suite, the smoke check and the
+CPU-baseline leg of the benchmark may load it; the product package never
+imports it.  Each C function cites the reference Rust file:line it restates.
+
+Parity pins: the reference (a Rust workspace) cannot be built here, so the
+restatement is pinned against the literal known answers of the reference's
+own unit tests (tests/golden/known_answers.json, tests/test_oracle_*.py), a
+brute-force edit-distance DP for both Myers formulations, and agreement of
+the i16 and i32 kernel flavours on the reference's seeded sweeps.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libesp_oracle.so")
+SOURCES = ["extend.c", "myers.c", "split.c", "batch.c"]
+
+OP_M, OP_I, OP_D, OP_N, OP_S = 0, 1, 2, 3, 4
+OP_CHARS = "MIDNS"
+EDIT_OFF, EDIT_AG, EDIT_TC = 0, 1, 2
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc into oracle/_build (portable C, -O2)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    srcs = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, "esp_oracle.h")]
+    if not force and os.path.exists(LIB_PATH):
+        lib_m = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(s) <= lib_m for s in srcs):
+            return LIB_PATH
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
+           "-o", LIB_PATH + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+class _Params(C.Structure):
+    _fields_ = [("match_score", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
+                ("gap_ext", C.c_int32), ("edit_dir", C.c_int32)]
+
+
+class _Ext(C.Structure):
+    _fields_ = [("read_start", C.c_uint32), ("read_end", C.c_uint32), ("ref_start", C.c_uint32),
+                ("score", C.c_int32), ("n_ops", C.c_uint32), ("cap", C.c_uint32),
+                ("ops", C.POINTER(C.c_uint32))]
+
+
+class _Touch(C.Structure):
+    _fields_ = [("touched", C.c_int32), ("row", C.c_int64), ("left", C.c_int32),
+                ("clamped", C.c_int32)]
+
+
+class _Contig(C.Structure):
+    _fields_ = [("len", C.c_uint32), ("packed", C.c_void_p), ("n_iv", C.c_void_p),
+                ("n_iv_count", C.c_uint32)]
+
+
+class _SpliceParams(C.Structure):
+    _fields_ = [("min_intron", C.c_uint32), ("max_intron", C.c_uint32),
+                ("gt_ag_bonus", C.c_int32), ("gc_ag_bonus", C.c_int32),
+                ("at_ac_bonus", C.c_int32), ("noncanonical_penalty", C.c_int32),
+                ("known_bonus", C.c_int32), ("refine_radius", C.c_uint32)]
+
+
+class _Junction(C.Structure):
+    _fields_ = [("start", C.c_uint32), ("end", C.c_uint32), ("minus_strand", C.c_int32)]
+
+
+class _Retry(C.Structure):
+    _fields_ = [("found", C.c_int32), ("dro", C.c_uint32), ("left_win_lo", C.c_uint32),
+                ("total", C.c_int32), ("left", _Ext), ("right", _Ext)]
+
+
+class _Rescue(C.Structure):
+    _fields_ = [("found", C.c_int32), ("cand", C.c_int32), ("dro", C.c_uint32),
+                ("pos", C.c_uint32), ("score", C.c_int32), ("signal", C.c_int32),
+                ("n_ops", C.c_uint32), ("cap", C.c_uint32), ("ops", C.POINTER(C.c_uint32))]
+
+
+class _Pairs(C.Structure):
+    _fields_ = [("seqs", C.c_void_p), ("read_off", C.c_void_p), ("read_len", C.c_void_p),
+                ("win_off", C.c_void_p), ("win_len", C.c_void_p), ("offset", C.c_void_p),
+                ("half", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        u8p = C.c_char_p
+        i64, i32 = C.c_int64, C.c_int32
+        L.orc_run_band.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), C.c_int, C.c_int,
+                                   i64, i64, i64, i64, C.POINTER(_Ext), C.POINTER(_Touch)]
+        L.orc_run_dispatch.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), C.c_int, i64,
+                                       i64, i64, i64, C.POINTER(_Ext), C.POINTER(_Touch)]
+        L.orc_extend.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), C.POINTER(_Ext)]
+        L.orc_extend_hint.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), i64, C.c_uint32,
+                                      C.c_uint32, C.POINTER(_Ext), C.POINTER(C.c_int)]
+        L.orc_band_cells.argtypes = [i64, i64, C.c_int, i64, i64]
+        L.orc_band_cells.restype = i64
+        L.orc_i16_add.argtypes = [C.c_int16, C.c_int16]
+        L.orc_i16_add.restype = C.c_int16
+        for name in ("orc_myers_infix_best_end", "orc_myers_infix_best_start",
+                     "orc_myers_long_infix_best_end", "orc_myers_long_infix_best_start",
+                     "orc_ea_edit_dp"):
+            getattr(L, name).argtypes = [u8p, i64, u8p, i64, C.POINTER(i32), C.POINTER(i64)]
+        for name in ("orc_myers_infix", "orc_myers_long_infix"):
+            getattr(L, name).argtypes = [u8p, i64, u8p, i64, C.POINTER(i32)]
+        for name in ("orc_engine_infix", "orc_engine_global"):
+            getattr(L, name).argtypes = [u8p, i64, u8p, i64, C.POINTER(C.c_uint32)]
+        L.orc_splice_signal.argtypes = [u8p, u8p, C.c_int]
+        L.orc_signal_score.argtypes = [C.c_int, C.POINTER(_SpliceParams)]
+        L.orc_junction_signal.argtypes = [C.POINTER(_Contig), C.POINTER(_Junction)]
+        L.orc_splice_params_default.argtypes = [C.POINTER(_SpliceParams)]
+        L.orc_cigar_ref_end.argtypes = [C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32]
+        L.orc_cigar_ref_end.restype = C.c_uint32
+        L.orc_retry_tail_start.argtypes = [C.POINTER(_Contig), u8p, C.c_uint32, C.c_uint32,
+                                           C.POINTER(_Junction), C.c_int, C.c_uint32,
+                                           C.POINTER(_SpliceParams), C.POINTER(_Params),
+                                           C.POINTER(_Retry)]
+        L.orc_channel_a.argtypes = [C.POINTER(_Contig), u8p, C.c_uint32, C.c_uint32, C.c_int,
+                                    C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.POINTER(_SpliceParams), C.POINTER(_Params),
+                                    C.POINTER(_Rescue)]
+        L.orc_slice_ascii.argtypes = [C.POINTER(_Contig), C.c_uint32, C.c_uint32, C.c_void_p]
+        L.orc_pack_2bit.argtypes = [u8p, i64, C.c_void_p]
+        L.orc_batch_extend.argtypes = [C.POINTER(_Pairs), i64, C.POINTER(_Params), C.c_int,
+                                       C.c_int] + [C.c_void_p] * 6 + [C.c_uint32, C.c_void_p]
+        L.orc_batch_extend.restype = i64
+        L.orc_batch_myers_best_end.argtypes = [C.c_void_p] * 5 + [i64, C.c_int, C.c_void_p,
+                                                                   C.c_void_p]
+        L.orc_batch_myers_best_end.restype = i64
+        L.free.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _libc_free(ptr):
+    C.CDLL(None).free(C.cast(ptr, C.c_void_p))
+
+
+@dataclass
+class Params:
+    """ExtendParams (crates/map/src/extend.rs:97-122)."""
+    match_score: int = 2
+    mismatch: int = -4
+    gap_open: int = 4
+    gap_ext: int = 2
+    edit_dir: int = EDIT_OFF
+
+    def c(self) -> _Params:
+        return _Params(self.match_score, self.mismatch, self.gap_open, self.gap_ext,
+                       self.edit_dir)
+
+
+@dataclass
+class Ext:
+    read_start: int
+    read_end: int
+    ref_start: int
+    score: int
+    cigar: List[Tuple[str, int]] = field(default_factory=list)
+
+    def key(self):
+        return (self.score, self.read_start, self.read_end, self.ref_start, tuple(self.cigar))
+
+
+@dataclass
+class Touch:
+    touched: bool
+    row: int
+    left: bool
+    clamped: bool
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def decode_ops(ops) -> List[Tuple[str, int]]:
+    return [(OP_CHARS[o & 15], o >> 4) for o in ops]
+
+
+def _b(s) -> bytes:
+    return s.encode() if isinstance(s, str) else bytes(s)
+
+
+def _call_ext(fn, *args, m: int, n: int):
+    cap = 2 * (m + n) + 8
+    buf = (C.c_uint32 * cap)()
+    e = _Ext(0, 0, 0, 0, 0, cap, buf)
+    rc = fn(*args, C.byref(e))
+    if rc != 0:
+        raise OracleError(f"oracle returned {rc}")
+    return Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops]))
+
+
+def run_band(read, win, params: Params = Params(), wide: bool = False,
+             band: Optional[Tuple[int, int]] = None) -> Tuple[Ext, Touch]:
+    """run_band<T> (extend.rs:606-851); band = (offset, half) or None."""
+    read, win = _b(read), _b(win)
+    p = params.c()
+    t = _Touch()
+    off, half = band if band is not None else (0, 0)
+    cap = 2 * (len(read) + len(win)) + 8
+    buf = (C.c_uint32 * cap)()
+    e = _Ext(0, 0, 0, 0, 0, cap, buf)
+    rc = lib().orc_run_band(read, len(read), win, len(win), C.byref(p), int(wide),
+                            int(band is not None), off, 1, 1, half, C.byref(e), C.byref(t))
+    if rc != 0:
+        raise OracleError(f"orc_run_band returned {rc}")
+    return (Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops])),
+            Touch(bool(t.touched), t.row, bool(t.left), bool(t.clamped)))
+
+
+def run_dispatch(read, win, params: Params = Params(),
+                 band: Optional[Tuple[int, int]] = None) -> Tuple[Ext, Touch]:
+    read, win = _b(read), _b(win)
+    p = params.c()
+    t = _Touch()
+    off, half = band if band is not None else (0, 0)
+    cap = 2 * (len(read) + len(win)) + 8
+    buf = (C.c_uint32 * cap)()
+    e = _Ext(0, 0, 0, 0, 0, cap, buf)
+    rc = lib().orc_run_dispatch(read, len(read), win, len(win), C.byref(p),
+                                int(band is not None), off, 1, 1, half, C.byref(e), C.byref(t))
+    if rc != 0:
+        raise OracleError(f"orc_run_dispatch returned {rc}")
+    return (Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops])),
+            Touch(bool(t.touched), t.row, bool(t.left), bool(t.clamped)))
+
+
+def extend(read, win, params: Params = Params()) -> Ext:
+    read, win = _b(read), _b(win)
+    p = params.c()
+    return _call_ext(lib().orc_extend, read, len(read), win, len(win), C.byref(p),
+                     m=len(read), n=len(win))
+
+
+def extend_hint(read, win, params: Params = Params(), offset: int = 0,
+                with_escalation: bool = False):
+    read, win = _b(read), _b(win)
+    p = params.c()
+    esc = C.c_int(0)
+    cap = 2 * (len(read) + len(win)) + 8
+    buf = (C.c_uint32 * cap)()
+    e = _Ext(0, 0, 0, 0, 0, cap, buf)
+    rc = lib().orc_extend_hint(read, len(read), win, len(win), C.byref(p), offset, 1, 1,
+                               C.byref(e), C.byref(esc))
+    if rc != 0:
+        raise OracleError(f"orc_extend_hint returned {rc}")
+    ext = Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops]))
+    return (ext, bool(esc.value)) if with_escalation else ext
+
+
+def band_cells(m: int, n: int, band: Optional[Tuple[int, int]]) -> int:
+    if band is None:
+        return lib().orc_band_cells(m, n, 0, 0, 0)
+    return lib().orc_band_cells(m, n, 1, band[0], band[1])
+
+
+def i16_add(a: int, b: int) -> int:
+    return lib().orc_i16_add(a, b)
+
+
+def _myers2(fn, read, text):
+    read, text = _b(read), _b(text)
+    d, e = C.c_int32(), C.c_int64()
+    rc = fn(read, len(read), text, len(text), C.byref(d), C.byref(e))
+    if rc != 0:
+        raise OracleError(f"myers oracle returned {rc}")
+    return d.value, e.value
+
+
+def myers_infix(read, text) -> int:
+    read, text = _b(read), _b(text)
+    d = C.c_int32()
+    rc = lib().orc_myers_infix(read, len(read), text, len(text), C.byref(d))
+    if rc != 0:
+        raise OracleError(f"orc_myers_infix returned {rc}")
+    return d.value
+
+
+def myers_long_infix(read, text) -> int:
+    read, text = _b(read), _b(text)
+    d = C.c_int32()
+    rc = lib().orc_myers_long_infix(read, len(read), text, len(text), C.byref(d))
+    if rc != 0:
+        raise OracleError(f"orc_myers_long_infix returned {rc}")
+    return d.value
+
+
+def myers_infix_best_end(read, text):
+    return _myers2(lib().orc_myers_infix_best_end, read, text)
+
+
+def myers_infix_best_start(read, text):
+    return _myers2(lib().orc_myers_infix_best_start, read, text)
+
+
+def myers_long_infix_best_end(read, text):
+    return _myers2(lib().orc_myers_long_infix_best_end, read, text)
+
+
+def myers_long_infix_best_start(read, text):
+    return _myers2(lib().orc_myers_long_infix_best_start, read, text)
+
+
+def ea_edit_dp(read, text):
+    return _myers2(lib().orc_ea_edit_dp, read, text)
+
+
+def engine_infix(read, text) -> int:
+    read, text = _b(read), _b(text)
+    d = C.c_uint32()
+    rc = lib().orc_engine_infix(read, len(read), text, len(text), C.byref(d))
+    if rc != 0:
+        raise OracleError(f"orc_engine_infix returned {rc}")
+    return d.value
+
+
+def engine_global(read, text) -> int:
+    read, text = _b(read), _b(text)
+    d = C.c_uint32()
+    rc = lib().orc_engine_global(read, len(read), text, len(text), C.byref(d))
+    if rc != 0:
+        raise OracleError(f"orc_engine_global returned {rc}")
+    return d.value
+
+
+# ---- reference storage / splice ----
+
+def pack_2bit(seq) -> bytes:
+    seq = _b(seq)
+    out = (C.c_uint8 * ((len(seq) + 3) // 4))()
+    lib().orc_pack_2bit(seq, len(seq), out)
+    return bytes(out)
+
+
+def n_intervals(seq) -> List[Tuple[int, int]]:
+    """Merged half-open runs of non-ACGT bytes (the contig's N list)."""
+    out: List[Tuple[int, int]] = []
+    s = None
+    for k, b in enumerate(_b(seq)):
+        isn = chr(b) not in "ACGTacgt"
+        if isn and s is None:
+            s = k
+        elif not isn and s is not None:
+            out.append((s, k))
+            s = None
+    if s is not None:
+        out.append((s, len(seq)))
+    return out
+
+
+class Contig:
+    """A 2-bit packed contig with N intervals (crates/map/src/fasta.rs:62-135)."""
+
+    def __init__(self, seq):
+        seq = _b(seq)
+        self.len = len(seq)
+        self.packed = pack_2bit(seq)
+        ivs = n_intervals(seq)
+        self._pk = (C.c_uint8 * max(1, len(self.packed))).from_buffer_copy(
+            self.packed or b"\0")
+        flat = [v for iv in ivs for v in iv]
+        self._iv = (C.c_uint32 * max(1, len(flat)))(*flat)
+        self.n_iv = ivs
+        self.c = _Contig(self.len, C.cast(self._pk, C.c_void_p), C.cast(self._iv, C.c_void_p),
+                         len(ivs))
+
+    def slice_ascii(self, start: int, end: int) -> bytes:
+        out = (C.c_uint8 * max(1, end - start))()
+        lib().orc_slice_ascii(C.byref(self.c), start, end, out)
+        return bytes(out[: end - start])
+
+
+SIG_GTAG, SIG_GCAG, SIG_ATAC, SIG_NONCANON = 0, 1, 2, 3
+
+
+def splice_params_default() -> _SpliceParams:
+    sp = _SpliceParams()
+    lib().orc_splice_params_default(C.byref(sp))
+    return sp
+
+
+def splice_signal(donor, acceptor, minus: bool) -> int:
+    return lib().orc_splice_signal(_b(donor), _b(acceptor), int(minus))
+
+
+def junction_signal(contig: Contig, start: int, end: int, minus: bool) -> int:
+    j = _Junction(start, end, int(minus))
+    return lib().orc_junction_signal(C.byref(contig.c), C.byref(j))
+
+
+def cigar_ref_end(pos: int, cigar: Sequence[Tuple[str, int]]) -> int:
+    ops = [(n << 4) | OP_CHARS.index(c) for c, n in cigar]
+    arr = (C.c_uint32 * max(1, len(ops)))(*ops)
+    return lib().orc_cigar_ref_end(pos, arr, len(ops))
+
+
+@dataclass
+class Retry:
+    dro: int
+    left_win_lo: int
+    total: int
+    left: Ext
+    right: Ext
+
+
+def retry_tail_start(contig: Contig, read, tail_start: int, start: int, end: int,
+                     minus: bool, signal: int, support: int,
+                     params: Params = Params()) -> Optional[Retry]:
+    """split.rs:150-223 retry_tail_start."""
+    read = _b(read)
+    sp = splice_params_default()
+    p = params.c()
+    j = _Junction(start, end, int(minus))
+    o = _Retry()
+    rc = lib().orc_retry_tail_start(C.byref(contig.c), read, len(read), tail_start,
+                                    C.byref(j), signal, support, C.byref(sp), C.byref(p),
+                                    C.byref(o))
+    if rc != 0:
+        raise OracleError(f"orc_retry_tail_start returned {rc}")
+    if not o.found:
+        return None
+    le = Ext(o.left.read_start, o.left.read_end, o.left.ref_start, o.left.score,
+             decode_ops(o.left.ops[: o.left.n_ops]))
+    re = Ext(o.right.read_start, o.right.read_end, o.right.ref_start, o.right.score,
+             decode_ops(o.right.ops[: o.right.n_ops]))
+    _libc_free(o.left.ops)
+    _libc_free(o.right.ops)
+    return Retry(o.dro, o.left_win_lo, o.total, le, re)
+
+
+@dataclass
+class Rescue:
+    cand: int
+    dro: int
+    pos: int
+    score: int
+    signal: int
+    cigar: List[Tuple[str, int]]
+
+
+def channel_a(contig: Contig, read, tail_start: int, minus: bool,
+              cands: Sequence[Tuple[int, int, bool]], support: Sequence[int],
+              params: Params = Params()) -> Optional[Rescue]:
+    """split.rs:468-570 channel A over caller-supplied candidates."""
+    read = _b(read)
+    sp = splice_params_default()
+    p = params.c()
+    js = (_Junction * max(1, len(cands)))(*[_Junction(s, e, int(mi)) for s, e, mi in cands])
+    sup = (C.c_uint32 * max(1, len(support)))(*support)
+    cap = 4 * len(read) + 16
+    buf = (C.c_uint32 * cap)()
+    o = _Rescue(0, 0, 0, 0, 0, 0, 0, cap, buf)
+    rc = lib().orc_channel_a(C.byref(contig.c), read, len(read), tail_start, int(minus),
+                             C.cast(js, C.c_void_p), C.cast(sup, C.c_void_p), len(cands),
+                             C.byref(sp), C.byref(p), C.byref(o))
+    if rc != 0:
+        raise OracleError(f"orc_channel_a returned {rc}")
+    if not o.found:
+        return None
+    return Rescue(o.cand, o.dro, o.pos, o.score, o.signal, decode_ops(buf[: o.n_ops]))
+
+
+# ---- batch drivers (CPU baseline) ----
+
+def batch_extend(seqs, read_off, read_len, win_off, win_len, offset, half, params: Params,
+                 mode: int, threads: int, ops_stride: int = 0):
+    """Run the oracle over a batch with `threads` workers.  Arrays are numpy.
+    mode 0 = run_dispatch with each pair's band (half < 0: full matrix),
+    mode 1 = extend_hint with each pair's offset.  Returns (cells, outputs)."""
+    import numpy as np
+    n = len(read_len)
+    keep = [np.ascontiguousarray(a) for a in (seqs, read_off.astype(np.uint64),
+                                               read_len.astype(np.uint32),
+                                               win_off.astype(np.uint64),
+                                               win_len.astype(np.uint32),
+                                               offset.astype(np.int64), half.astype(np.int32))]
+    pr = _Pairs(*[a.ctypes.data for a in keep])
+    score = np.zeros(n, np.int32)
+    rs = np.zeros(n, np.uint32)
+    re = np.zeros(n, np.uint32)
+    fs = np.zeros(n, np.uint32)
+    nops = np.zeros(n, np.uint32)
+    touched = np.zeros(n, np.int32)
+    ops = np.zeros(max(1, n * ops_stride), np.uint32) if ops_stride else None
+    p = params.c()
+    cells = lib().orc_batch_extend(C.byref(pr), n, C.byref(p), mode, threads,
+                                   score.ctypes.data, rs.ctypes.data, re.ctypes.data,
+                                   fs.ctypes.data, nops.ctypes.data,
+                                   ops.ctypes.data if ops is not None else None, ops_stride,
+                                   touched.ctypes.data)
+    if cells < 0:
+        raise OracleError(f"orc_batch_extend returned {cells}")
+    out = dict(score=score, read_start=rs, read_end=re, ref_start=fs, n_ops=nops,
+               touched=touched)
+    if ops is not None:
+        out["ops"] = ops.reshape(n, ops_stride)
+    return int(cells), out
+
+
+def batch_myers_best_end(seqs, read_off, read_len, text_off, text_len, threads: int):
+    import numpy as np
+    n = len(read_len)
+    keep = [np.ascontiguousarray(a) for a in (seqs, read_off.astype(np.uint64),
+                                               read_len.astype(np.uint32),
+                                               text_off.astype(np.uint64),
+                                               text_len.astype(np.uint32))]
+    dist = np.zeros(n, np.int32)
+    end = np.zeros(n, np.int64)
+    cells = lib().orc_batch_myers_best_end(*[a.ctypes.data for a in keep], n, threads,
+                                           dist.ctypes.data, end.ctypes.data)
+    if cells < 0:
+        raise OracleError(f"orc_batch_myers_best_end returned {cells}")
+    return int(cells), dist, end
