@@ -1,0 +1,114 @@
+"""ctypes binding of the C ABI in include/esperanto_gb300.h.
+
+The shared library is built in-tree (esperanto_gb300/_lib) by
+esperanto_gb300.build.  There is no CPU fallback: if the library is missing
+or fails to load, every entry point raises NativeUnavailable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+ESP_OK = 0
+ESP_EINVAL = -1
+ESP_ECUDA = -2
+ESP_ECAP = -3
+ESP_EDOMAIN = -4
+ESP_ENOMEM = -5
+ESP_EBUSY = -6
+ESP_ETIMEOUT = -7
+ESP_ECLOSED = -8
+
+MODE_BAND = 0
+MODE_HINT = 1
+
+
+class NativeUnavailable(RuntimeError):
+    """The GB300 extension library is not built or cannot be loaded."""
+
+
+class EspError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"esperanto_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class ExtendParamsC(C.Structure):
+    _fields_ = [("match_score", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
+                ("gap_ext", C.c_int32), ("edit_dir", C.c_int32)]
+
+
+class ExtensionC(C.Structure):
+    _fields_ = [("read_start", C.c_uint32), ("read_end", C.c_uint32), ("ref_start", C.c_uint32),
+                ("score", C.c_int32), ("n_ops", C.c_uint32), ("touch_row", C.c_int32),
+                ("touched", C.c_uint8), ("touch_left", C.c_uint8),
+                ("touch_clamped", C.c_uint8), ("escalated", C.c_uint8), ("status", C.c_int32)]
+
+
+class PairC(C.Structure):
+    _fields_ = [("read_pos", C.c_uint64), ("win_pos", C.c_uint64), ("read_len", C.c_uint32),
+                ("win_len", C.c_uint32), ("band_offset", C.c_int32), ("band_half", C.c_int32),
+                ("n_first", C.c_uint32), ("n_read", C.c_uint16), ("n_win", C.c_uint16)]
+
+
+class BatchLimitsC(C.Structure):
+    _fields_ = [("max_read_len", C.c_uint32), ("max_win_len", C.c_uint32),
+                ("max_half", C.c_int32)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load (building first if stale) the extension library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    try:
+        path = _build.build()
+    except Exception as e:  # nvcc missing or failing: no silent fallback
+        if os.path.exists(_build.LIB):
+            path = _build.LIB
+        else:
+            raise NativeUnavailable(f"cannot build the GB300 extension: {e}") from e
+    try:
+        L = C.CDLL(path)
+    except OSError as e:
+        raise NativeUnavailable(f"cannot load {path}: {e}") from e
+    vp, sz, u8p = C.c_void_p, C.c_size_t, C.c_char_p
+    L.esp_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.esp_destroy.argtypes = [vp]
+    L.esp_last_error.argtypes = [vp]
+    L.esp_last_error.restype = C.c_char_p
+    L.esp_stream.argtypes = [vp]
+    L.esp_stream.restype = vp
+    L.esp_last_launch_count.argtypes = [vp]
+    L.esp_last_launch_count.restype = C.c_uint64
+    ext_args = [vp, u8p, sz, u8p, sz, C.POINTER(ExtendParamsC)]
+    L.esp_extend.argtypes = ext_args + [C.POINTER(ExtensionC), vp, C.c_uint32]
+    L.esp_extend_hint.argtypes = ext_args + [C.c_int64, C.c_uint32, C.c_uint32,
+                                             C.POINTER(ExtensionC), vp, C.c_uint32]
+    L.esp_run_band.argtypes = ext_args + [C.c_int64, C.c_int64, C.POINTER(ExtensionC), vp,
+                                          C.c_uint32]
+    L.esp_batch_extend_host.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                        C.c_uint64, C.POINTER(ExtendParamsC), vp, vp, C.c_uint32]
+    L.esp_batch_extend_device.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                          C.c_uint64, C.POINTER(BatchLimitsC),
+                                          C.POINTER(ExtendParamsC), vp, vp, C.c_uint32, vp]
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    """Names declared in include/esperanto_gb300.h (for the load test)."""
+    import re
+    hdr = os.path.join(_build.ROOT, "include", "esperanto_gb300.h")
+    with open(hdr) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^\s*(?:[\w ]+\*?\s*)\b(esp_\w+)\s*\(", text, re.M)))

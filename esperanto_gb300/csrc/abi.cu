@@ -1,0 +1,434 @@
+// abi.cu -- the C ABI: handles, the per-call drop-ins of extend.rs and the
+// batch-submit API.  Host-side code only; kernels live in gotoh.cu etc.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "esp_internal.h"
+#include "esperanto_gb300.h"
+
+struct esp_handle {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+    int gotoh_bps = 0;  // resident DP blocks per SM (queried once)
+    uint64_t scratch_budget = 8ull << 30;  // bytes of DP scratch one launch may use
+    // grow-only device buffers
+    void *d_in = nullptr;       // per-call staging: pair | n intervals | arena
+    size_t d_in_cap = 0;
+    void *d_res = nullptr;      // per-call results: esp_extension | cigar
+    size_t d_res_cap = 0;
+    uint32_t *d_tb = nullptr;
+    size_t d_tb_cap = 0;        // words
+    uint32_t *d_rb = nullptr;
+    size_t d_rb_cap = 0;
+    uint32_t *d_esc = nullptr;  // escalation list
+    size_t d_esc_cap = 0;       // bytes
+    uint32_t *d_ctr = nullptr;  // [0..1] queues (u64), [4] esc count
+    // host pinned staging
+    void *h_in = nullptr;
+    size_t h_in_cap = 0;
+    void *h_res = nullptr;
+    size_t h_res_cap = 0;
+    // host batch staging for esp_batch_extend_host
+    void *d_bat = nullptr;
+    size_t d_bat_cap = 0;
+};
+
+namespace {
+
+int fail(esp_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_fail(esp_handle *h, cudaError_t e, const char *what) {
+    return fail(h, ESP_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, expr)                                        \
+    do {                                                   \
+        cudaError_t _e = (expr);                           \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, #expr); \
+    } while (0)
+
+int grow_device(esp_handle *h, void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ESP_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t sz = std::max(need, (size_t)4096);
+    cudaError_t e = cudaMalloc(p, sz);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, ESP_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    *cap = sz;
+    return ESP_OK;
+}
+
+int grow_host(esp_handle *h, void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ESP_OK;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t sz = std::max(need * 2, (size_t)65536);
+    cudaError_t e = cudaMallocHost(p, sz);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, ESP_ENOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    *cap = sz;
+    return ESP_OK;
+}
+
+// extend.rs:150-159 base_code folded to the 2-bit arena plus N intervals.
+int ascii_code(uint8_t b) {
+    switch (b) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return 4;
+    }
+}
+
+// Append `len` ASCII bases at arena base position `pos` and their N runs.
+void encode_seq(const uint8_t *s, size_t len, uint8_t *arena, uint64_t pos,
+                std::vector<esp_n_interval> &iv) {
+    size_t k = 0;
+    while (k < len) {
+        int c = ascii_code(s[k]);
+        if (c == 4) {
+            size_t e = k;
+            while (e < len && ascii_code(s[e]) == 4) e++;
+            iv.push_back({(uint32_t)k, (uint32_t)e});
+            k = e;
+            continue;
+        }
+        uint64_t p = pos + k;
+        arena[p >> 2] |= (uint8_t)(c << (6 - 2 * (p & 3)));
+        k++;
+    }
+}
+
+struct Limits {
+    uint64_t tb_words = 1, rb_words = 1;
+    uint32_t max_m = 0;
+};
+
+void add_limits(Limits &L, uint32_t m, uint32_t n, int32_t half) {
+    uint64_t tb, rb;
+    esp::gotoh_scratch_words(m, n, half, tb, rb);
+    L.tb_words = std::max(L.tb_words, tb);
+    L.rb_words = std::max(L.rb_words, rb);
+    L.max_m = std::max(L.max_m, m);
+}
+
+// Enqueue the DP launches of one batch whose inputs are on the device.
+int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_pairs,
+                  const uint8_t *d_arena, uint64_t arena_bytes, const esp_n_interval *d_iv,
+                  uint64_t n_iv, const esp::GotohConst &K, const Limits &L1, const Limits &L2,
+                  esp_extension *d_out, uint32_t *d_cigar, uint32_t cigar_stride,
+                  cudaStream_t st) {
+    h->launches = 0;
+    if (n_pairs == 0) return ESP_OK;
+    if (n_pairs > 0xffffffffull - 64) return fail(h, ESP_EINVAL, "batch too large");
+    int rc;
+    // scratch slots: one warp per 32 pairs up to the resident limit, bounded
+    // by the scratch budget
+    uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
+    uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
+    uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
+    if (h->gotoh_bps == 0) h->gotoh_bps = esp::gotoh_blocks_per_sm(128);
+    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * h->gotoh_bps * 4);
+    uint64_t need_warps = (n_pairs + 31) / 32;
+    uint64_t warps = std::min(want, need_warps);
+    uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes);
+    warps = std::min(warps, budget_warps);
+    warps = (warps + 3) / 4 * 4;  // whole 128-thread blocks: every launched warp owns a slot
+    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * tbw * 32 * 4)) != ESP_OK)
+        return rc;
+    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * rbw * 32 * 4)) != ESP_OK)
+        return rc;
+    if (mode == ESP_MODE_HINT &&
+        (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
+        return rc;
+    CK(h, cudaMemsetAsync(h->d_ctr, 0, 64, st));
+    esp::GotohJob job{};
+    job.pairs = d_pairs;
+    job.n_pairs = n_pairs;
+    job.arena = d_arena;
+    job.arena_bases = arena_bytes * 4;
+    job.n_iv = d_iv;
+    job.n_iv_count = n_iv;
+    job.out = d_out;
+    job.cigar = d_cigar;
+    job.cigar_stride = cigar_stride;
+    job.tb = h->d_tb;
+    job.tb_words = tbw;
+    job.rb = h->d_rb;
+    job.rb_words = rbw;
+    job.queue = h->d_ctr;
+    job.esc_list = h->d_esc;
+    job.esc_count = h->d_ctr + 4;
+    job.mode = mode == ESP_MODE_HINT ? 1 : 0;
+    job.max_m = (int)L1.max_m;
+    CK(h, esp::launch_gotoh(job, K, (int)warps, 128, st));
+    h->launches++;
+    if (mode == ESP_MODE_HINT) {
+        esp::GotohJob j2 = job;
+        j2.mode = 2;
+        j2.list = h->d_esc;
+        j2.list_count = h->d_ctr + 4;
+        j2.queue = h->d_ctr + 2;
+        CK(h, esp::launch_gotoh(j2, K, (int)warps, 128, st));
+        h->launches++;
+    }
+    return ESP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int esp_create(esp_handle **out, int device) {
+    if (!out) return ESP_EINVAL;
+    *out = nullptr;
+    esp_handle *h = new (std::nothrow) esp_handle();
+    if (!h) return ESP_ENOMEM;
+    h->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_ctr, 64);
+    if (e != cudaSuccess) {
+        delete h;
+        return ESP_ECUDA;
+    }
+    *out = h;
+    return ESP_OK;
+}
+
+int esp_destroy(esp_handle *h) {
+    if (!h) return ESP_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->d_in);
+    cudaFree(h->d_res);
+    cudaFree(h->d_tb);
+    cudaFree(h->d_rb);
+    cudaFree(h->d_esc);
+    cudaFree(h->d_ctr);
+    cudaFree(h->d_bat);
+    if (h->h_in) cudaFreeHost(h->h_in);
+    if (h->h_res) cudaFreeHost(h->h_res);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return ESP_OK;
+}
+
+const char *esp_last_error(const esp_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+void *esp_stream(esp_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+uint64_t esp_last_launch_count(const esp_handle *h) { return h ? h->launches : 0; }
+
+}  // extern "C"
+
+// One pair from ASCII through the device path (the per-call drop-in).
+static int one_pair(esp_handle *h, int mode, const uint8_t *read, size_t m, const uint8_t *win,
+                    size_t n, const esp_extend_params *params, int64_t offset, int64_t half,
+                    esp_extension *out, uint32_t *cigar, uint32_t cap) {
+    if (!h || !params || !out || (m && !read) || (n && !win)) return fail(h, ESP_EINVAL, "null argument");
+    if (m > 32767 || n > 32767) return fail(h, ESP_EDOMAIN, "sequence longer than 32767");
+    if (offset < -(1ll << 30) || offset > (1ll << 30)) return fail(h, ESP_EDOMAIN, "band offset out of range");
+    if (half > (1ll << 30)) half = 1ll << 30;
+    esp::GotohConst K;
+    if (esp::make_gotoh_const(*params, K) != ESP_OK)
+        return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
+    CK(h, cudaSetDevice(h->device));
+    std::vector<esp_n_interval> iv;
+    uint64_t wpos = ((m + 63) / 64) * 64;  // window starts on a 16-byte boundary
+    uint64_t bases = wpos + n;
+    size_t arena_bytes = ((bases + 3) / 4 + 15) / 16 * 16 + 16;
+    size_t hdr = 64 + 8 * (m + n + 2);  // pair + worst-case N intervals
+    hdr = (hdr + 255) / 256 * 256;
+    int rc;
+    if ((rc = grow_host(h, &h->h_in, &h->h_in_cap, hdr + arena_bytes)) != ESP_OK) return rc;
+    uint8_t *hin = (uint8_t *)h->h_in;
+    uint8_t *harena = hin + hdr;
+    memset(harena, 0, arena_bytes);
+    encode_seq(read, m, harena, 0, iv);
+    size_t n_read_iv = iv.size();
+    encode_seq(win, n, harena, wpos, iv);
+    esp_pair P{};
+    P.read_pos = 0;
+    P.win_pos = wpos;
+    P.read_len = (uint32_t)m;
+    P.win_len = (uint32_t)n;
+    P.band_offset = (int32_t)offset;
+    P.band_half = half < 0 ? -1 : (int32_t)half;
+    P.n_first = 0;
+    if (n_read_iv > 65535 || iv.size() - n_read_iv > 65535)
+        return fail(h, ESP_EDOMAIN, "too many N runs");
+    P.n_read = (uint16_t)n_read_iv;
+    P.n_win = (uint16_t)(iv.size() - n_read_iv);
+    memcpy(hin, &P, sizeof(P));
+    if (!iv.empty()) memcpy(hin + 64, iv.data(), iv.size() * sizeof(esp_n_interval));
+    if ((rc = grow_device(h, &h->d_in, &h->d_in_cap, hdr + arena_bytes)) != ESP_OK) return rc;
+    uint32_t stride = std::max<uint32_t>(cap, 1) + 8;
+    size_t res_bytes = 64 + (size_t)stride * 4;
+    if ((rc = grow_device(h, &h->d_res, &h->d_res_cap, res_bytes)) != ESP_OK) return rc;
+    if ((rc = grow_host(h, &h->h_res, &h->h_res_cap, res_bytes)) != ESP_OK) return rc;
+    cudaStream_t st = h->stream;
+    CK(h, cudaMemcpyAsync(h->d_in, hin, hdr + arena_bytes, cudaMemcpyHostToDevice, st));
+    uint8_t *din = (uint8_t *)h->d_in;
+    Limits L1, L2;
+    if (mode == ESP_MODE_HINT) {
+        add_limits(L1, (uint32_t)m, (uint32_t)n, 30);
+        add_limits(L2, (uint32_t)m, (uint32_t)n, -1);
+    } else {
+        add_limits(L1, (uint32_t)m, (uint32_t)n, P.band_half);
+    }
+    esp_extension *dout = (esp_extension *)h->d_res;
+    uint32_t *dcig = (uint32_t *)((uint8_t *)h->d_res + 64);
+    rc = enqueue_batch(h, mode, (const esp_pair *)din, 1, din + hdr, arena_bytes - 16,
+                       (const esp_n_interval *)(din + 64), iv.size(), K, L1, L2, dout, dcig,
+                       stride, st);
+    if (rc != ESP_OK) return rc;
+    CK(h, cudaMemcpyAsync(h->h_res, h->d_res, res_bytes, cudaMemcpyDeviceToHost, st));
+    CK(h, cudaStreamSynchronize(st));
+    esp_extension r;
+    memcpy(&r, h->h_res, sizeof(r));
+    if (r.status == ESP_EINVAL) return fail(h, ESP_EINVAL, "kernel refused the pair");
+    *out = r;
+    uint32_t k = std::min<uint32_t>(r.n_ops, cap);
+    if (r.status == ESP_OK && cigar && k) memcpy(cigar, (uint8_t *)h->h_res + 64, k * 4);
+    if (r.n_ops > cap) {
+        out->status = ESP_ECAP;
+        return fail(h, ESP_ECAP, "CIGAR buffer too small");
+    }
+    return ESP_OK;
+}
+
+extern "C" {
+
+int esp_extend(esp_handle *h, const uint8_t *read, size_t read_len, const uint8_t *ref_window,
+               size_t window_len, const esp_extend_params *params, esp_extension *out,
+               uint32_t *cigar, uint32_t cigar_cap) {
+    return one_pair(h, ESP_MODE_BAND, read, read_len, ref_window, window_len, params, 0, -1, out,
+                    cigar, cigar_cap);
+}
+
+int esp_extend_hint(esp_handle *h, const uint8_t *read, size_t read_len,
+                    const uint8_t *ref_window, size_t window_len,
+                    const esp_extend_params *params, int64_t hint_offset, uint32_t hint_num,
+                    uint32_t hint_den, esp_extension *out, uint32_t *cigar,
+                    uint32_t cigar_cap) {
+    // run_band asserts num == den == 1 (extend.rs:633); den 0 counts as 1.
+    if (hint_num != 1 || (hint_den > 1)) return fail(h, ESP_EINVAL, "DiagHint slope must be 1/1");
+    return one_pair(h, ESP_MODE_HINT, read, read_len, ref_window, window_len, params, hint_offset,
+                    30, out, cigar, cigar_cap);
+}
+
+int esp_run_band(esp_handle *h, const uint8_t *read, size_t read_len, const uint8_t *ref_window,
+                 size_t window_len, const esp_extend_params *params, int64_t band_offset,
+                 int64_t band_half, esp_extension *out, uint32_t *cigar, uint32_t cigar_cap) {
+    return one_pair(h, ESP_MODE_BAND, read, read_len, ref_window, window_len, params,
+                    band_half < 0 ? 0 : band_offset, band_half, out, cigar, cigar_cap);
+}
+
+static int batch_common(esp_handle *h, int mode, const esp_pair *pairs_host, uint64_t n_pairs,
+                        Limits &L1, Limits &L2) {
+    for (uint64_t k = 0; k < n_pairs; k++) {
+        const esp_pair &P = pairs_host[k];
+        if (mode == ESP_MODE_HINT) {
+            add_limits(L1, P.read_len, P.win_len, P.win_len <= 30 ? -1 : 30);
+            add_limits(L2, P.read_len, P.win_len, -1);
+        } else {
+            add_limits(L1, P.read_len, P.win_len, P.band_half);
+        }
+    }
+    return ESP_OK;
+}
+
+int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
+                          const uint8_t *arena, uint64_t arena_bytes,
+                          const esp_n_interval *n_iv, uint64_t n_iv_count,
+                          const esp_extend_params *params, esp_extension *out,
+                          uint32_t *cigar, uint32_t cigar_stride) {
+    if (!h || !params || !out || (n_pairs && (!pairs || !arena))) return fail(h, ESP_EINVAL, "null argument");
+    if (mode != ESP_MODE_BAND && mode != ESP_MODE_HINT) return fail(h, ESP_EINVAL, "bad mode");
+    esp::GotohConst K;
+    if (esp::make_gotoh_const(*params, K) != ESP_OK)
+        return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
+    CK(h, cudaSetDevice(h->device));
+    Limits L1, L2;
+    batch_common(h, mode, pairs, n_pairs, L1, L2);
+    size_t sz_pairs = (n_pairs * sizeof(esp_pair) + 255) / 256 * 256;
+    size_t sz_iv = (n_iv_count * sizeof(esp_n_interval) + 255) / 256 * 256;
+    size_t sz_arena = (arena_bytes + 16 + 255) / 256 * 256;
+    size_t sz_out = (n_pairs * sizeof(esp_extension) + 255) / 256 * 256;
+    size_t sz_cig = (n_pairs * (size_t)cigar_stride * 4 + 255) / 256 * 256;
+    int rc;
+    if ((rc = grow_device(h, &h->d_bat, &h->d_bat_cap, sz_pairs + sz_iv + sz_arena + sz_out + sz_cig)) != ESP_OK)
+        return rc;
+    uint8_t *b = (uint8_t *)h->d_bat;
+    esp_pair *dp = (esp_pair *)b;
+    esp_n_interval *div = (esp_n_interval *)(b + sz_pairs);
+    uint8_t *da = b + sz_pairs + sz_iv;
+    esp_extension *dout = (esp_extension *)(da + sz_arena);
+    uint32_t *dcig = (uint32_t *)((uint8_t *)dout + sz_out);
+    cudaStream_t st = h->stream;
+    CK(h, cudaMemcpyAsync(dp, pairs, n_pairs * sizeof(esp_pair), cudaMemcpyHostToDevice, st));
+    if (n_iv_count)
+        CK(h, cudaMemcpyAsync(div, n_iv, n_iv_count * sizeof(esp_n_interval), cudaMemcpyHostToDevice, st));
+    CK(h, cudaMemcpyAsync(da, arena, arena_bytes, cudaMemcpyHostToDevice, st));
+    CK(h, cudaMemsetAsync(da + arena_bytes, 0, 16, st));
+    rc = enqueue_batch(h, mode, dp, n_pairs, da, arena_bytes, div, n_iv_count, K, L1, L2, dout,
+                       dcig, cigar_stride, st);
+    if (rc != ESP_OK) return rc;
+    CK(h, cudaMemcpyAsync(out, dout, n_pairs * sizeof(esp_extension), cudaMemcpyDeviceToHost, st));
+    if (cigar && cigar_stride)
+        CK(h, cudaMemcpyAsync(cigar, dcig, n_pairs * (size_t)cigar_stride * 4, cudaMemcpyDeviceToHost, st));
+    CK(h, cudaStreamSynchronize(st));
+    return ESP_OK;
+}
+
+int esp_batch_extend_device(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
+                            const uint8_t *arena, uint64_t arena_bytes,
+                            const esp_n_interval *n_iv, uint64_t n_iv_count,
+                            const esp_batch_limits *limits, const esp_extend_params *params,
+                            esp_extension *out, uint32_t *cigar, uint32_t cigar_stride,
+                            void *stream) {
+    if (!h || !params || !out || !limits || (n_pairs && (!pairs || !arena)))
+        return fail(h, ESP_EINVAL, "null argument");
+    if (mode != ESP_MODE_BAND && mode != ESP_MODE_HINT) return fail(h, ESP_EINVAL, "bad mode");
+    if (limits->max_read_len > 32767 || limits->max_win_len > 32767)
+        return fail(h, ESP_EDOMAIN, "sequence longer than 32767");
+    esp::GotohConst K;
+    if (esp::make_gotoh_const(*params, K) != ESP_OK)
+        return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
+    CK(h, cudaSetDevice(h->device));
+    Limits L1, L2;
+    if (mode == ESP_MODE_HINT) {
+        add_limits(L1, limits->max_read_len, limits->max_win_len, 30);
+        add_limits(L2, limits->max_read_len, limits->max_win_len, -1);
+    } else {
+        add_limits(L1, limits->max_read_len, limits->max_win_len,
+                   limits->max_half < 0 ? -1 : limits->max_half);
+    }
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    return enqueue_batch(h, mode, pairs, n_pairs, arena, arena_bytes, n_iv, n_iv_count, K, L1, L2,
+                         out, cigar, cigar_stride, st);
+}
+
+}  // extern "C"

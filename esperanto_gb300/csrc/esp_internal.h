@@ -1,0 +1,66 @@
+// esp_internal.h -- host-side internal interfaces between the ABI layer and
+// the kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "esperanto_gb300.h"
+
+namespace esp {
+
+// Device copy of the scoring constants (derived once per call from
+// esp_extend_params; see gotoh.cu for the scaled-key arithmetic).
+struct GotohConst {
+    int32_t oe1;        // 4*open_ext - 1  (E open key, low bits 01)
+    int32_t oe4;        // 4*open_ext      (F open key, low bits 10 after + Hp)
+    int32_t ex4;        // 4*ext
+    int32_t open_ext;   // -(gap_open + gap_ext)
+    int32_t ext;        // -gap_ext
+    int32_t match;      // match_score
+    int32_t edit_dir;
+    uint32_t lut4[5][2];  // per read code: bytes = 4*score vs ref codes 0..7 (4..7 = N)
+    int8_t lut[25];       // SubstLut scores[read*5 + ref] (raw, for traceback deltas)
+};
+
+// Validate parameters against the device domain and fill the constants.
+// Returns ESP_OK or ESP_EDOMAIN.
+int make_gotoh_const(const esp_extend_params &p, GotohConst &k);
+
+// Work description for one DP launch.
+struct GotohJob {
+    const esp_pair *pairs;      // device
+    uint64_t n_pairs;
+    const uint32_t *list;       // optional: indices into pairs (device); null = 0..n-1
+    const uint32_t *list_count; // optional device counter (when list is a queue)
+    const uint8_t *arena;
+    uint64_t arena_bases;       // bases addressable in the arena (excluding padding)
+    const esp_n_interval *n_iv;
+    uint64_t n_iv_count;
+    int mode;                   // 0 band/full per pair, 1 hint attempt 1, 2 hint attempt 2
+    uint32_t *esc_list;         // mode 1: escalated pairs are appended here
+    uint32_t *esc_count;
+    esp_extension *out;
+    uint32_t *cigar;
+    uint32_t cigar_stride;
+    uint32_t *tb;               // traceback scratch: slots * tb_words * 32 words
+    uint64_t tb_words;          // per-thread words (>= max strips * strip stride)
+    uint32_t *rb;               // row-buffer scratch: slots * rb_words * 32 words
+    uint64_t rb_words;
+    uint32_t *queue;            // device work counter (zeroed before launch)
+    int max_m;                  // largest read length in the job
+};
+
+// Launch the persistent DP kernel with `warps` warps total.
+cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, int block,
+                         cudaStream_t st);
+
+// Resident blocks per SM of the DP kernel at `block` threads.
+int gotoh_blocks_per_sm(int block);
+
+// Traceback and row-buffer words one thread needs for a pair.
+void gotoh_scratch_words(uint32_t m, uint32_t n, int32_t half, uint64_t &tb, uint64_t &rb);
+
+}  // namespace esp

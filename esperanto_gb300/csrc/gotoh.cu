@@ -1,0 +1,648 @@
+// gotoh.cu -- GB300 banded / full-matrix affine-gap (Gotoh) local alignment
+// with traceback to CIGAR, bit-exact with the reference's scalar kernel
+// (crates/map/src/extend.rs:606-1068).
+//
+// Execution model: one thread owns one read x window pair (inter-sequence
+// parallelism).  A warp takes 32 consecutive entries of a length-sorted work
+// list from a device queue (persistent kernel), so the lanes of a warp run the
+// same loop trip counts and their scratch accesses coalesce.
+//
+// DP layout: the matrix is swept in strips of 8 rows.  Inside a strip the
+// thread walks the strip's column range left to right and evaluates the 8
+// cells of each column top to bottom, all in registers:
+//   * H/F of column j-1 for each of the 8 rows ride in registers (left deps),
+//   * H/E of the row above the strip come from a per-thread row buffer (one
+//     packed int16x2 word per column) that the strip's last row rewrites in
+//     place, so row-buffer traffic is 8 bytes per column per 8 cells,
+//   * the 4 traceback bits of the 8 cells are packed into one 32-bit word
+//     per (strip, column): 2 bits H source per row in the low half-word and
+//     (E opened, F opened) per row in the high half-word.
+//
+// Scaled-key arithmetic (what makes the reference's tie cascade cheap):
+// every score is held as 4*v plus a 2-bit tag so that a plain integer max
+// performs both the value comparison and the reference's tie preference.
+//   H is held as Hp = 4H + 2.
+//   E key: max(Hp_up + 4*open_ext - 1, E4_up + 4*ext): low bit 1 <=> opened,
+//          and an open/extend tie resolves to "open" as `better` (strict >)
+//          does at extend.rs:731.
+//   F key: max(Hp_left + 4*open_ext, F4_left + 4*ext): bit 1 <=> opened.
+//   H key: max(4*diag + 2, 4E + 1, 4F + 0, 3): among equal values diag
+//          beats E beats F (the cascade order of extend.rs:764-777), and the
+//          START tag 3 wins whenever the maximum is 0 (the zero-floor rewrite
+//          of extend.rs:780-782).  hsrc = key & 3: 3 start, 2 diag, 1 E, 0 F.
+// Out-of-window cells present H = 0, E = F = NEG to their neighbours exactly
+// as the scalar kernel's margins do (extend.rs:718-759).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "esp_device.cuh"
+#include "esp_internal.h"
+
+namespace esp {
+
+static constexpr int NEG4 = -32768;  // E/F sentinel in scaled units (int16 min)
+static constexpr int STRIP = 8;
+
+struct Geo {
+    int off, half, n;
+    __device__ __forceinline__ int c(int i) const {
+        int x = off + i;
+        return x < 1 ? 1 : (x > n ? n : x);
+    }
+    __device__ __forceinline__ int lo(int i) const {
+        int v = c(i) - half;
+        return v > 1 ? v : 1;
+    }
+    __device__ __forceinline__ int hi(int i) const {
+        int v = c(i) + half;
+        return v < n ? v : n;
+    }
+};
+
+struct Seq {
+    const uint8_t *arena;
+    uint64_t pos;
+    const esp_n_interval *iv;
+    uint32_t cnt;
+    __device__ __forceinline__ uint32_t code(int64_t q) const {
+        return code5(arena, pos, iv, cnt, q);
+    }
+};
+
+struct Strip {
+    int Hl[STRIP], Fl[STRIP], rk[STRIP], hr[STRIP];
+    uint32_t l0[STRIP], l1[STRIP];
+    int lo[STRIP], hi[STRIP];
+};
+
+// One column of one strip.  upH/upE enter as the row above the strip at
+// column j and leave as the strip's last row at column j; `diag` is the row
+// above at column j-1.  Returns the column's packed traceback word.
+template <bool MASKED>
+__device__ __forceinline__ uint32_t dp_column(Strip &S, const GotohConst &K, int j, uint32_t sel,
+                                              int cj, int &upH, int &upE, int diag) {
+    uint32_t wa = 0, wb = 0;
+    int d = diag;
+#pragma unroll
+    for (int r = 0; r < STRIP; r++) {
+        int left = S.Hl[r];
+        int kE = max(upH + K.oe1, upE + K.ex4);
+        int kF = max(left + K.oe4, S.Fl[r] + K.ex4);
+        int E4 = kE & ~3;
+        int F4 = kF & ~3;
+        int kd = d + prmt_sx(S.l0[r], S.l1[r], sel);
+        int key = max(max(kd, kE | 1), max(F4, 3));
+        int Hp = (key & ~3) | 2;
+        wa = (wa << 2) | (uint32_t)(key & 3);
+        wb = (wb << 2) | (uint32_t)((kE & 1) | (kF & 2));
+        if (MASKED) {
+            bool in = (j >= S.lo[r]) & (j <= S.hi[r]);
+            if (j == S.hi[r]) S.hr[r] = Hp;
+            if (in) {
+                S.rk[r] = max(S.rk[r], (Hp << 15) + cj);
+            } else {
+                Hp = 2;
+                E4 = NEG4;
+                F4 = NEG4;
+            }
+        } else {
+            S.rk[r] = max(S.rk[r], (Hp << 15) + cj);
+        }
+        d = left;
+        S.Hl[r] = Hp;
+        S.Fl[r] = F4;
+        upH = Hp;
+        upE = E4;
+    }
+    return __byte_perm(wa, wb, 0x5410);
+}
+
+struct FillResult {
+    int bestHp, best_i, best_j;
+    int trow;
+    bool tleft, tclamp;
+};
+
+// Column range [a, b] of a strip, MASKED or not.
+template <bool MASKED>
+__device__ __forceinline__ void dp_range(Strip &S, const GotohConst &K, int a, int b, int &diag,
+                                         uint32_t &cw, uint32_t &nm, int &kk, const Seq &win,
+                                         const uint32_t *rb, int plo, int phi, bool have_prev,
+                                         uint32_t *rbw, int lo7, bool write_rb, uint32_t *tbp,
+                                         int clo) {
+    for (int j = a; j <= b; j++) {
+        if (kk == 16) {
+            cw = load16(win.arena, win.pos + (uint64_t)(j - 1));
+            nm = win.cnt ? nmask16(win.iv, win.cnt, j - 1) : 0u;
+            kk = 0;
+        }
+        uint32_t code = (cw >> 30) | ((nm >> 29) & 4u);
+        cw <<= 2;
+        nm <<= 1;
+        kk++;
+        uint32_t sel = code * 0x1111u + 0x8880u;
+        int bH = 2, bE = NEG4;
+        if (have_prev && j <= phi) {
+            uint32_t w = rb[(size_t)(j - plo) * 32];
+            bH = (int)(w & 0xffffu);
+            bE = ((int)w) >> 16;
+        }
+        int upH = bH, upE = bE;
+        uint32_t word = dp_column<MASKED>(S, K, j, sel, 32767 - j, upH, upE, diag);
+        diag = bH;
+        if (write_rb && j >= lo7)
+            rbw[(size_t)(j - lo7) * 32] = __byte_perm((uint32_t)upH, (uint32_t)upE, 0x5410);
+        tbp[(size_t)(j - clo) * 32] = word;
+    }
+}
+
+// Fill the DP for one pair; traceback words land in tb (stride sw per strip).
+__device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ s_lut, int m,
+                              int n, const Geo &g, const Seq &read, const Seq &win,
+                              uint32_t *tb, int sw, uint32_t *rb) {
+    FillResult R;
+    R.bestHp = 2;
+    R.best_i = 0;
+    R.best_j = 0;
+    R.trow = 0;
+    R.tleft = false;
+    R.tclamp = false;
+    int nstrips = (m + STRIP - 1) / STRIP;
+    int plo = 0, phi = -1;
+    Strip S;
+    for (int s = 0; s < nstrips; s++) {
+        int i0 = s * STRIP + 1;
+        int nact = min(STRIP, m - i0 + 1);
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            S.lo[r] = g.lo(i0 + r);
+            S.hi[r] = g.hi(i0 + r);
+            S.Hl[r] = 2;
+            S.Fl[r] = NEG4;
+            S.rk[r] = -1;
+            S.hr[r] = -1;
+        }
+        int clo = S.lo[0];
+        int chi = g.hi(i0 + nact - 1);
+        int lo7 = S.lo[STRIP - 1];
+        int hi0 = S.hi[0];
+        // read codes of the strip's rows -> per-row substitution words
+        uint32_t rw = load16(read.arena, read.pos + (uint64_t)(i0 - 1));
+        uint32_t rn = read.cnt ? nmask16(read.iv, read.cnt, i0 - 1) : 0u;
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            uint32_t c = (rw >> (30 - 2 * r)) & 3u;
+            if ((rn >> (31 - r)) & 1u) c = 4;
+            S.l0[r] = s_lut[2 * c];
+            S.l1[r] = s_lut[2 * c + 1];
+        }
+        bool have_prev = s > 0;
+        int diag = 2;
+        if (have_prev && clo - 1 >= plo && clo - 1 <= phi)
+            diag = (int)(rb[(size_t)(clo - 1 - plo) * 32] & 0xffffu);
+        uint32_t cw = 0, nm = 0;
+        int kk = 16;
+        bool write_rb = s + 1 < nstrips;
+        uint32_t *tbp = tb + (size_t)s * sw * 32;
+        int a_end = min(lo7, chi);
+        dp_range<true>(S, K, clo, a_end, diag, cw, nm, kk, win, rb, plo, phi, have_prev, rb, lo7,
+                       write_rb, tbp, clo);
+        int b_end = min(hi0 - 1, chi);
+        dp_range<false>(S, K, lo7 + 1, b_end, diag, cw, nm, kk, win, rb, plo, phi, have_prev, rb,
+                        lo7, write_rb, tbp, clo);
+        int c_beg = max(lo7 + 1, hi0);
+        dp_range<true>(S, K, c_beg, chi, diag, cw, nm, kk, win, rb, plo, phi, have_prev, rb, lo7,
+                       write_rb, tbp, clo);
+        // row bookkeeping in row order (extend.rs:795-827)
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            if (r < nact) {
+                int rowHp = S.rk[r] >> 15;
+                int argj = 32767 - (S.rk[r] & 32767);
+                if (R.trow == 0) {
+                    if (argj == S.lo[r]) {  // H at the left edge is the row max
+                        R.trow = i0 + r;
+                        R.tleft = true;
+                        R.tclamp = S.lo[r] <= 1;
+                    } else if (S.hi[r] < n && S.hr[r] == rowHp) {
+                        R.trow = i0 + r;
+                        R.tleft = false;
+                        R.tclamp = S.hi[r] >= n;
+                    }
+                }
+                if (rowHp > R.bestHp) {
+                    R.bestHp = rowHp;
+                    R.best_i = i0 + r;
+                    R.best_j = argj;
+                }
+            }
+        }
+        plo = lo7;
+        phi = S.hi[STRIP - 1];
+    }
+    return R;
+}
+
+__device__ __forceinline__ bool neutral_col(uint32_t q, uint32_t r) {
+    return q < 4 && r < 4 && (q == r || (r == 0 && q == 2) || (r == 3 && q == 1));
+}
+
+// One traceback step from (i, j) in `state` (0 H, 1 E, 2 F).  Returns false
+// when the walk stops (extend.rs:884-930).
+struct Step {
+    int op, d;
+};
+
+__device__ __forceinline__ bool tb_step(const GotohConst &K, const int8_t *__restrict__ lut,
+                                        const Geo &g, const uint32_t *tb, int sw, const Seq &read,
+                                        const Seq &win, int &i, int &j, int &state, Step &st) {
+    if (i <= 0 || j <= 0) return false;
+    if (j < g.lo(i) || j > g.hi(i)) return false;
+    int s = (i - 1) >> 3, r = (i - 1) & 7;
+    int clo = g.lo(s * STRIP + 1);
+    uint32_t w = tb[((size_t)s * sw + (size_t)(j - clo)) * 32];
+    int sh = 2 * (7 - r);
+    uint32_t hsrc = (w >> sh) & 3u;
+    uint32_t eo = (w >> (16 + sh)) & 1u;
+    uint32_t fo = (w >> (17 + sh)) & 1u;
+    if (state == 0) {
+        if (hsrc == 2u) {
+            uint32_t q = read.code(i - 1), rc = win.code(j - 1);
+            st.op = ESP_OP_M;
+            st.d = lut[q * 5 + rc];
+            i--;
+            j--;
+        } else if (hsrc == 1u) {
+            st.op = ESP_OP_I;
+            st.d = K.open_ext;
+            state = eo ? 0 : 1;
+            i--;
+        } else if (hsrc == 0u) {
+            st.op = ESP_OP_D;
+            st.d = K.open_ext;
+            state = fo ? 0 : 2;
+            j--;
+        } else {
+            return false;  // H_START
+        }
+    } else if (state == 1) {
+        st.op = ESP_OP_I;
+        st.d = K.ext;
+        if (eo) state = 0;
+        i--;
+    } else {
+        st.op = ESP_OP_D;
+        st.d = K.ext;
+        if (fo) state = 0;
+        j--;
+    }
+    return true;
+}
+
+struct CigarOut {
+    uint32_t *p;
+    uint32_t cap;
+    uint32_t n;
+    bool overflow;
+    __device__ __forceinline__ void put(uint32_t idx, uint32_t v) {
+        if (idx < cap) p[idx] = v;
+        else overflow = true;
+    }
+};
+
+// Traceback, end trimming, rebuild and neutral flanks (extend.rs:864-1068).
+__device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, const Geo &g,
+                          const uint32_t *tb, int sw, int m, int n, const Seq &read,
+                          const Seq &win, const FillResult &F, esp_extension &o, uint32_t *cig,
+                          uint32_t cap) {
+    // walk 1: number of steps N, total T, trail
+    int N = 0, P = 0, trail = 0;
+    {
+        int i = F.best_i, j = F.best_j, state = 0;
+        Step st;
+        while (tb_step(K, lut, g, tb, sw, read, win, i, j, state, st)) {
+            P += st.d;
+            N++;
+            if (P <= 0) trail = N;
+        }
+    }
+    const int T = P;
+    uint32_t read_start, ref_start, read_end, ref_end;
+    int score = 0;
+    CigarOut co{cig, cap, 0, false};
+    uint32_t K_runs = 0;  // kept runs, written from index 2 in walk order
+    int first_op = -1, last_op = -1;  // forward order first / last kept op
+    if (N == 0) {
+        read_start = (uint32_t)max(F.best_i, 0);
+        ref_start = (uint32_t)max(F.best_j, 0);
+        read_end = read_start;
+        ref_end = ref_start;
+    } else {
+        // Walk 2.  With walk-order prefix sums P_t, the reference's forward
+        // lead is N-1-u where u is the first index in [-1, N-2] with
+        // P_u >= T (P_-1 = 0), so the kept steps are walk indices
+        // [trail, u]; lead + trail >= N (the degenerate keep-the-middle
+        // case, extend.rs:956-960) is exactly u < trail.  Step t* (the
+        // middle step) is captured on the way in case that happens.
+        bool degenerate = (T <= 0);  // u = -1
+        const int tstar = N - 1 - N / 2;
+        int i = F.best_i, j = F.best_j, state = 0;
+        int pos_acc = 0;
+        bool found = false;
+        int cur_op = -1;
+        uint32_t cur_len = 0;
+        read_end = ref_end = read_start = ref_start = 0;
+        int ts_ib = 0, ts_jb = 0, ts_ia = 0, ts_ja = 0, ts_op = 0, ts_d = 0;
+        bool done = false;
+        for (int t = 0; t < N && !done; t++) {
+            int i_before = i, j_before = j;
+            Step st;
+            tb_step(K, lut, g, tb, sw, read, win, i, j, state, st);
+            if (t == tstar) {
+                ts_ib = i_before;
+                ts_jb = j_before;
+                ts_ia = i;
+                ts_ja = j;
+                ts_op = st.op;
+                ts_d = st.d;
+            }
+            pos_acc += st.d;
+            if (!degenerate && !found && t <= N - 2 && pos_acc >= T) {
+                found = true;
+                if (t < trail) degenerate = true;  // nothing emitted yet
+            }
+            if (degenerate) {
+                if (t >= tstar) done = true;
+                continue;
+            }
+            if (t >= trail) {
+                if (t == trail) {
+                    read_end = (uint32_t)i_before;
+                    ref_end = (uint32_t)j_before;
+                    last_op = st.op;
+                }
+                score += st.d;
+                if (st.op == cur_op) {
+                    cur_len++;
+                } else {
+                    if (cur_op >= 0) co.put(2 + K_runs++, (cur_len << 4) | (uint32_t)cur_op);
+                    cur_op = st.op;
+                    cur_len = 1;
+                }
+                first_op = st.op;
+                if (found) {  // t == u_min: the kept region starts here
+                    read_start = (uint32_t)i;
+                    ref_start = (uint32_t)j;
+                    done = true;
+                }
+            }
+        }
+        if (degenerate) {
+            read_end = (uint32_t)ts_ib;
+            ref_end = (uint32_t)ts_jb;
+            read_start = (uint32_t)ts_ia;
+            ref_start = (uint32_t)ts_ja;
+            score = ts_d;
+            co.put(2, (1u << 4) | (uint32_t)ts_op);
+            K_runs = 1;
+            first_op = last_op = ts_op;
+        } else {
+            if (cur_op >= 0) co.put(2 + K_runs++, (cur_len << 4) | (uint32_t)cur_op);
+            if (!found) {  // lead = 0: kept through the last step
+                read_start = (uint32_t)i;
+                ref_start = (uint32_t)j;
+            }
+        }
+    }
+    // reverse the kept runs into forward order
+    if (!co.overflow) {
+        for (uint32_t a = 0, b = K_runs ? K_runs - 1 : 0; a < b; a++, b--) {
+            uint32_t t = cig[2 + a];
+            cig[2 + a] = cig[2 + b];
+            cig[2 + b] = t;
+        }
+    }
+    // neutral flanks (extend.rs:991-1049)
+    uint32_t nl = 0, nr = 0;
+    if (score > 0) {
+        int delta = 0;
+        uint32_t lim = min(read_start, ref_start);
+        for (uint32_t k = 1; k <= lim; k++) {
+            uint32_t q = read.code((int64_t)read_start - k), r = win.code((int64_t)ref_start - k);
+            if (!neutral_col(q, r)) break;
+            delta += lut[q * 5 + r];
+            if (delta == 0) nl = k;
+        }
+        delta = 0;
+        uint32_t av = min((uint32_t)m - read_end, (uint32_t)n - ref_end);
+        for (uint32_t k = 0; k < av; k++) {
+            uint32_t q = read.code((int64_t)read_end + k), r = win.code((int64_t)ref_end + k);
+            if (!neutral_col(q, r)) break;
+            delta += lut[q * 5 + r];
+            if (delta == 0) nr = k + 1;
+        }
+        read_start -= nl;
+        ref_start -= nl;
+        read_end += nr;
+    }
+    // final CIGAR: S, M(neutral), kept runs, M(neutral), S (push_op merging)
+    uint32_t total = K_runs;
+    if (nl > 0 && first_op != ESP_OP_M) total++;
+    if (nr > 0 && last_op != ESP_OP_M) total++;
+    if (read_start > 0) total++;
+    if (read_end < (uint32_t)m) total++;
+    if (!co.overflow && total <= cap) {
+        uint32_t w = 0;
+        int prev = -1;
+        auto push = [&](uint32_t op, uint32_t len) {
+            if ((int)op == prev) {
+                cig[w - 1] += len << 4;
+            } else {
+                cig[w++] = (len << 4) | op;
+                prev = (int)op;
+            }
+        };
+        if (read_start > 0) push(ESP_OP_S, read_start);
+        if (nl > 0) push(ESP_OP_M, nl);
+        for (uint32_t k = 0; k < K_runs; k++) {
+            uint32_t v = cig[2 + k];
+            push(v & 15u, v >> 4);
+        }
+        if (nr > 0) push(ESP_OP_M, nr);
+        if (read_end < (uint32_t)m) push(ESP_OP_S, (uint32_t)m - read_end);
+        o.status = ESP_OK;
+    } else {
+        o.status = ESP_ECAP;
+    }
+    o.n_ops = total;
+    o.read_start = read_start;
+    o.read_end = read_end;
+    o.ref_start = ref_start;
+    o.score = score;
+}
+
+__device__ void process_pair(const GotohJob &job, const GotohConst &K,
+                             const uint32_t *__restrict__ s_lut, const int8_t *__restrict__ lut,
+                             uint32_t pi, uint32_t *tb, uint32_t *rb) {
+    if (pi >= job.n_pairs) return;  // corrupt work list: never index past the batch
+    esp_pair P = job.pairs[pi];
+    int m = (int)P.read_len, n = (int)P.win_len;
+    esp_extension o;
+    o.read_start = o.read_end = o.ref_start = 0;
+    o.score = 0;
+    o.n_ops = 0;
+    o.touch_row = 0;
+    o.touched = o.touch_left = o.touch_clamped = 0;
+    o.escalated = job.mode == 2 ? 1 : 0;
+    o.status = ESP_OK;
+    uint32_t *cig = job.cigar + (uint64_t)pi * job.cigar_stride;
+    if (m == 0 || n == 0) {  // extend.rs:430-442 empty_extension
+        if (m > 0) {
+            o.n_ops = 1;
+            if (job.cigar_stride >= 1) cig[0] = ((uint32_t)m << 4) | ESP_OP_S;
+            else o.status = ESP_ECAP;
+        }
+        job.out[pi] = o;
+        return;
+    }
+    Geo g;
+    bool full;
+    if (job.mode == 0) {
+        full = P.band_half < 0;
+        g.off = full ? 0 : P.band_offset;
+        g.half = full ? n : P.band_half;
+    } else if (job.mode == 1) {
+        full = 30 >= n;  // INITIAL_BAND >= window: full matrix, accepted directly
+        g.off = full ? 0 : P.band_offset;
+        g.half = full ? n : 30;
+    } else {
+        full = true;
+        g.off = 0;
+        g.half = n;
+    }
+    g.n = n;
+    int sw = full ? n : min(2 * g.half + STRIP, n);
+    uint64_t need_tb = (uint64_t)((m + STRIP - 1) / STRIP) * (uint64_t)sw;
+    uint64_t need_rb = (uint64_t)min(2 * g.half + 1, n);
+    if (need_tb > job.tb_words || need_rb > job.rb_words) {
+        o.status = ESP_EINVAL;  // scratch sized too small by the host: refuse, never overrun
+        job.out[pi] = o;
+        return;
+    }
+    if ((uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
+        P.read_pos + (uint64_t)m > job.arena_bases || P.win_pos + (uint64_t)n > job.arena_bases ||
+        m > 32767 || n > 32767) {
+        o.status = ESP_EINVAL;  // pair outside the arena / N table: refuse
+        job.out[pi] = o;
+        return;
+    }
+    const esp_n_interval *iv = job.n_iv + P.n_first;
+    Seq read{job.arena, P.read_pos, iv, P.n_read};
+    Seq win{job.arena, P.win_pos, iv + P.n_read, P.n_win};
+    FillResult F = dp_fill(K, s_lut, m, n, g, read, win, tb, sw, rb);
+    dp_finish(K, lut, g, tb, sw, m, n, read, win, F, o, cig, job.cigar_stride);
+    if (F.trow) {
+        o.touched = 1;
+        o.touch_row = F.trow;
+        o.touch_left = F.tleft ? 1 : 0;
+        o.touch_clamped = F.tclamp ? 1 : 0;
+    }
+    if (job.mode == 1 && !full) {
+        // extend.rs:421-426: escalate on a band-edge touch or < 85% of perfect
+        int perfect = m * K.match;
+        if (F.trow != 0 || o.score * 20 < perfect * 17) {
+            uint32_t slot = atomicAdd(job.esc_count, 1u);
+            job.esc_list[slot] = pi;
+            o.escalated = 1;
+        }
+    }
+    job.out[pi] = o;
+}
+
+__global__ void __launch_bounds__(128, 4) gotoh_kernel(GotohJob job, GotohConst K) {
+    __shared__ uint32_t s_lut[10];
+    __shared__ int8_t s_lut25[32];
+    if (threadIdx.x == 0) {  // static indices keep the parameter block out of local memory
+#pragma unroll
+        for (int k = 0; k < 10; k++) s_lut[k] = K.lut4[k >> 1][k & 1];
+#pragma unroll
+        for (int k = 0; k < 25; k++) s_lut25[k] = K.lut[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp_slot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t *tb = job.tb + warp_slot * job.tb_words * 32 + lane;
+    uint32_t *rb = job.rb + warp_slot * job.rb_words * 32 + lane;
+    const uint64_t total = job.list_count ? (uint64_t)(*job.list_count) : job.n_pairs;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd((unsigned long long *)job.queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        uint64_t k = base + lane;
+        if (k < total) {
+            uint32_t pi = job.list ? job.list[k] : (uint32_t)k;
+            process_pair(job, K, s_lut, s_lut25, pi, tb, rb);
+        }
+    }
+}
+
+int make_gotoh_const(const esp_extend_params &p, GotohConst &k) {
+    // Device domain: substitution scores fit the 4*s int8 PRMT table and the
+    // scaled gap keys fit int16 in the row buffer.  The reference's own
+    // parameter sets (defaults 2/-4/4/2 and the 400/400 rescue pass) are inside.
+    auto in8 = [](int v) { return v >= -32 && v <= 31; };
+    if (!in8(p.match_score) || !in8(p.mismatch) || p.gap_open < 0 || p.gap_ext < 0 ||
+        4LL * (p.gap_open + p.gap_ext) > 8000 || p.edit_dir < 0 || p.edit_dir > 2)
+        return ESP_EDOMAIN;
+    k.open_ext = -(p.gap_open + p.gap_ext);
+    k.ext = -p.gap_ext;
+    k.oe1 = 4 * k.open_ext - 1;
+    k.oe4 = 4 * k.open_ext;
+    k.ex4 = 4 * k.ext;
+    k.match = p.match_score;
+    k.edit_dir = p.edit_dir;
+    // SubstLut (extend.rs:164-179): scores[read*5 + ref]
+    int lut[25];
+    for (int i = 0; i < 25; i++) lut[i] = (int16_t)p.mismatch;
+    for (int c = 0; c < 4; c++) lut[c * 5 + c] = (int16_t)p.match_score;
+    if (p.edit_dir == ESP_EDIT_AG) lut[10] = 0;  // read G / ref A
+    if (p.edit_dir == ESP_EDIT_TC) lut[8] = 0;   // read C / ref T
+    for (int i = 0; i < 25; i++) k.lut[i] = (int8_t)lut[i];
+    for (int rc = 0; rc < 5; rc++) {
+        uint32_t w[2] = {0, 0};
+        for (int fc = 0; fc < 8; fc++) {
+            int s = lut[rc * 5 + (fc < 4 ? fc : 4)];
+            w[fc >> 2] |= (uint32_t)(uint8_t)(int8_t)(4 * s) << (8 * (fc & 3));
+        }
+        k.lut4[rc][0] = w[0];
+        k.lut4[rc][1] = w[1];
+    }
+    return ESP_OK;
+}
+
+void gotoh_scratch_words(uint32_t m, uint32_t n, int32_t half, uint64_t &tb, uint64_t &rb) {
+    bool full = half < 0;
+    int64_t h = full ? n : half;
+    int64_t sw = full ? n : (2 * h + STRIP < (int64_t)n ? 2 * h + STRIP : (int64_t)n);
+    tb = (uint64_t)((m + STRIP - 1) / STRIP) * (uint64_t)sw;
+    rb = (uint64_t)(2 * h + 1 < (int64_t)n ? 2 * h + 1 : (int64_t)n);
+}
+
+int gotoh_blocks_per_sm(int block) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel, block, 0) != cudaSuccess)
+        return 1;
+    return nb > 0 ? nb : 1;
+}
+
+cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, int block,
+                         cudaStream_t st) {
+    int threads = warps * 32;
+    int grid = (threads + block - 1) / block;
+    gotoh_kernel<<<grid, block, 0, st>>>(job, k);
+    return cudaGetLastError();
+}
+
+}  // namespace esp

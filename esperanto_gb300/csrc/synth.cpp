@@ -1,0 +1,188 @@
+// synth.cpp -- deterministic synthetic workloads (host side, multi-threaded).
+//
+// The reference ships no datasets for this path (all of its own test inputs
+// are generated, crates/map/src/extend.rs:2481-2525), so every benchmark
+// configuration is a seeded generator.  Each pair draws from its own
+// splitmix64 stream seeded by (seed, pair index), so generation is
+// parallel and independent of the thread count.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "esperanto_gb300.h"
+
+namespace {
+
+struct Rng {
+    uint64_t s;
+    explicit Rng(uint64_t seed) : s(seed) {}
+    uint64_t next() {  // splitmix64
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    uint32_t below(uint32_t n) { return (uint32_t)(((next() >> 32) * (uint64_t)n) >> 32); }
+    double unit() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    uint8_t base() { return (uint8_t)(next() >> 62); }
+};
+
+uint64_t pair_seed(uint64_t seed, uint64_t idx) {
+    Rng r(seed * 0x2545F4914F6CDD1Dull + idx * 0x9E3779B97F4A7C15ull + 0x1234567ull);
+    r.next();
+    return r.next();
+}
+
+void put2(uint8_t *arena, uint64_t p, uint8_t c) {
+    arena[p >> 2] |= (uint8_t)(c << (6 - 2 * (p & 3)));
+}
+
+// Error model shared by the Gotoh configurations: 1% substitutions, 0.1%
+// indels (half insertions, half deletions) of geometric length 1..3, and
+// A->G at 5% of A positions on forward-strand pairs (T->C on reverse-strand
+// pairs, chosen 50/50 per pair).
+void derive_read(Rng &rng, const uint8_t *win, uint32_t n, uint32_t s0, uint32_t L,
+                 uint8_t *out) {
+    bool fwd = rng.next() & 1;
+    uint32_t s = s0, k = 0;
+    while (k < L) {
+        double u = rng.unit();
+        if (u < 0.001) {
+            uint32_t len = 1;
+            while (len < 3 && (rng.next() & 1)) len++;
+            if (u < 0.0005) {
+                for (uint32_t t = 0; t < len && k < L; t++) out[k++] = rng.base();
+                continue;
+            }
+            s += len;
+            continue;
+        }
+        uint8_t b = s < n ? win[s] : rng.base();
+        s++;
+        if (rng.unit() < 0.01) {
+            b = (uint8_t)((b + 1 + rng.below(3)) & 3);
+        } else if (fwd && b == 0 && rng.unit() < 0.05) {
+            b = 2;  // A -> G
+        } else if (!fwd && b == 3 && rng.unit() < 0.05) {
+            b = 1;  // T -> C
+        }
+        out[k++] = b;
+    }
+}
+
+struct Shape {
+    uint32_t L, n, half;
+};
+
+// Config 0: 150-bp reads from a 214-bp window at offset 32, band half 32.
+// Config 2: L ~ U[50,300], half from {16,32,64,128} w.p. {.4,.3,.2,.1},
+//           window L + 2*half, read drawn at offset `half`.
+Shape shape_of(int config, Rng &rng) {
+    if (config == 0) return {150, 214, 32};
+    uint32_t L = 50 + rng.below(251);
+    double u = rng.unit();
+    uint32_t h = u < 0.4 ? 16 : (u < 0.7 ? 32 : (u < 0.9 ? 64 : 128));
+    return {L, L + 2 * h, h};
+}
+
+template <class F>
+void parallel_for(uint64_t n, F f) {
+    unsigned T = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    if (n < 4096) T = 1;
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < T; t++)
+        th.emplace_back([&, t] {
+            uint64_t lo = n * t / T, hi = n * (t + 1) / T;
+            for (uint64_t i = lo; i < hi; i++) f(i);
+        });
+    for (auto &x : th) x.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+// Sizes of a Gotoh workload: total arena bytes (including 16 bytes of
+// padding) for `n_pairs` pairs of configuration 0 or 2.
+int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int config, uint64_t *arena_bytes) {
+    if (!arena_bytes || (config != 0 && config != 2)) return ESP_EINVAL;
+    std::vector<uint64_t> bases(n_pairs);
+    parallel_for(n_pairs, [&](uint64_t i) {
+        Rng r(pair_seed(seed, i));
+        Shape s = shape_of(config, r);
+        bases[i] = s.L + s.n;
+    });
+    uint64_t tot = 0;
+    for (uint64_t b : bases) tot += b;
+    *arena_bytes = (tot + 3) / 4 + 16;
+    return ESP_OK;
+}
+
+// Fill a Gotoh workload: pairs[i] gets the read and window of pair i packed
+// into `arena` (zeroed by this call), band offset/half of the configuration.
+int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
+                    uint64_t arena_bytes, esp_pair *pairs) {
+    if (!arena || !pairs || (config != 0 && config != 2)) return ESP_EINVAL;
+    std::vector<Shape> shp(n_pairs);
+    parallel_for(n_pairs, [&](uint64_t i) {
+        Rng r(pair_seed(seed, i));
+        shp[i] = shape_of(config, r);
+    });
+    std::vector<uint64_t> pos(n_pairs + 1, 0);
+    for (uint64_t i = 0; i < n_pairs; i++) pos[i + 1] = pos[i] + shp[i].L + shp[i].n;
+    if ((pos[n_pairs] + 3) / 4 + 16 > arena_bytes) return ESP_EINVAL;
+    memset(arena, 0, arena_bytes);
+    // Sequences are packed back to back, so the first and last byte of a
+    // thread's contiguous pair range may be shared with a neighbour thread;
+    // those bytes are collected and OR-ed in a serial pass afterwards.
+    unsigned T = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    if (n_pairs < 4096) T = 1;
+    std::vector<std::vector<std::pair<uint64_t, uint8_t>>> edge(T);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < T; t++)
+        th.emplace_back([&, t] {
+            uint64_t lo = n_pairs * t / T, hi = n_pairs * (t + 1) / T;
+            std::vector<uint8_t> win, rd;
+            uint64_t first_byte = pos[lo] >> 2, last_byte = pos[hi] >> 2;
+            for (uint64_t i = lo; i < hi; i++) {
+                Rng r(pair_seed(seed, i));
+                Shape s = shape_of(config, r);  // same draws as the sizing pass
+                win.resize(s.n);
+                rd.resize(s.L);
+                for (uint32_t k = 0; k < s.n; k++) win[k] = r.base();
+                derive_read(r, win.data(), s.n, s.half, s.L, rd.data());
+                uint64_t p = pos[i];
+                for (uint32_t k = 0; k < s.L; k++, p++) {
+                    uint64_t b = p >> 2;
+                    uint8_t v = (uint8_t)(rd[k] << (6 - 2 * (p & 3)));
+                    if (b == first_byte || b == last_byte) edge[t].push_back({b, v});
+                    else arena[b] |= v;
+                }
+                for (uint32_t k = 0; k < s.n; k++, p++) {
+                    uint64_t b = p >> 2;
+                    uint8_t v = (uint8_t)(win[k] << (6 - 2 * (p & 3)));
+                    if (b == first_byte || b == last_byte) edge[t].push_back({b, v});
+                    else arena[b] |= v;
+                }
+                esp_pair &P = pairs[i];
+                P.read_pos = pos[i];
+                P.win_pos = pos[i] + s.L;
+                P.read_len = s.L;
+                P.win_len = s.n;
+                P.band_offset = (int32_t)s.half;
+                P.band_half = (int32_t)s.half;
+                P.n_first = 0;
+                P.n_read = 0;
+                P.n_win = 0;
+            }
+        });
+    for (auto &x : th) x.join();
+    for (auto &e : edge)
+        for (auto &bv : e) arena[bv.first] |= bv.second;
+    return ESP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,188 @@
+/*
+ * esperanto_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * ESPERANTO read-alignment inner loop.
+ *
+ * The entry points mirror the reference's Rust functions one for one (each
+ * declaration cites the function it replaces, by path:line within the
+ * reference project) so that a thin FFI shim can keep the reference's
+ * signatures.  Everything is plain C: pointers, sizes and PODs; no CUDA or
+ * PyTorch types cross the boundary.  Streams are passed as `void *`
+ * (a cudaStream_t, NULL = the handle's own stream).
+ *
+ * Conventions
+ *   - Return value: ESP_OK (0) or a negative ESP_E* status.  The reference's
+ *     functions are infallible; a nonzero status here means a CUDA error, a
+ *     full output buffer, or an argument outside the supported domain.
+ *   - Sequences at the per-call entry points are ASCII bytes exactly as the
+ *     reference receives them (`&[u8]`); bases are folded by the reference's
+ *     base_code (A/a=0 C/c=1 G/g=2 T/t=3, anything else 4).
+ *   - CIGAR ops are u32 `(len << 4) | code` with code M=0 I=1 D=2 N=3 S=4.
+ *   - Handles are not thread-safe; use one handle per host thread (the
+ *     reference keeps one ExtendBuffer per rayon worker).
+ */
+#ifndef ESPERANTO_GB300_H
+#define ESPERANTO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ESP_OK 0
+#define ESP_EINVAL (-1)   /* bad argument                                    */
+#define ESP_ECUDA (-2)    /* CUDA runtime error (see esp_last_error)         */
+#define ESP_ECAP (-3)     /* CIGAR output buffer too small                   */
+#define ESP_EDOMAIN (-4)  /* parameters outside the device kernels' domain   */
+#define ESP_ENOMEM (-5)   /* device or host allocation failed                */
+#define ESP_EBUSY (-6)    /* admission refused (serve loop over budget)      */
+#define ESP_ETIMEOUT (-7) /* bounded wait expired                            */
+#define ESP_ECLOSED (-8)  /* queue closed                                    */
+
+#define ESP_OP_M 0
+#define ESP_OP_I 1
+#define ESP_OP_D 2
+#define ESP_OP_N 3
+#define ESP_OP_S 4
+
+#define ESP_EDIT_OFF 0 /* EditDir::Off */
+#define ESP_EDIT_AG 1  /* EditDir::Ag  */
+#define ESP_EDIT_TC 2  /* EditDir::Tc  */
+
+typedef struct esp_handle esp_handle;
+
+/* crates/map/src/extend.rs:97-122 ExtendParams */
+typedef struct {
+    int32_t match_score; /* reward, e.g. 2                 */
+    int32_t mismatch;    /* stored negative, e.g. -4        */
+    int32_t gap_open;    /* stored positive, e.g. 4         */
+    int32_t gap_ext;     /* stored positive, e.g. 2         */
+    int32_t edit_dir;    /* ESP_EDIT_*                      */
+} esp_extend_params;
+
+/* crates/map/src/extend.rs:200-229 Extension + TouchRec (the CIGAR goes to a
+ * separate caller buffer). */
+typedef struct {
+    uint32_t read_start;
+    uint32_t read_end;
+    uint32_t ref_start;
+    int32_t score;
+    uint32_t n_ops;      /* full CIGAR length, even when larger than the buffer */
+    int32_t touch_row;   /* TouchRec.row (0 when untouched)                     */
+    uint8_t touched;     /* TouchRec.touched                                    */
+    uint8_t touch_left;  /* TouchRec.left                                       */
+    uint8_t touch_clamped;
+    uint8_t escalated;   /* extend_hint ran attempt 2 (full matrix)             */
+    int32_t status;      /* ESP_OK or ESP_ECAP for this pair                    */
+} esp_extension;
+
+/* ---- handle ---- */
+
+/* Create a handle bound to CUDA device `device` (its own stream, pinned
+ * staging and grow-only device scratch).  Replaces the reference's
+ * per-thread ExtendBuffer (crates/map/src/extend.rs:231-251). */
+int esp_create(esp_handle **out, int device);
+int esp_destroy(esp_handle *h);
+/* Message of the last error on this handle (static storage of the handle). */
+const char *esp_last_error(const esp_handle *h);
+/* The handle's CUDA stream (cudaStream_t as void *). */
+void *esp_stream(esp_handle *h);
+
+/* ---- per-call drop-ins: crates/map/src/extend.rs ---- */
+
+/* extend (extend.rs:347-354): full-window local alignment. */
+int esp_extend(esp_handle *h, const uint8_t *read, size_t read_len, const uint8_t *ref_window,
+               size_t window_len, const esp_extend_params *params, esp_extension *out,
+               uint32_t *cigar, uint32_t cigar_cap);
+
+/* extend_hint (extend.rs:392-428): banded attempt of half-width 30 around
+ * the hint diagonal, escalating to the full matrix on a band-edge touch or a
+ * score below 85% of perfect.  num/den follow DiagHint (den 0 counts as 1;
+ * every reference call site passes 1/1, and run_band asserts it). */
+int esp_extend_hint(esp_handle *h, const uint8_t *read, size_t read_len,
+                    const uint8_t *ref_window, size_t window_len,
+                    const esp_extend_params *params, int64_t hint_offset, uint32_t hint_num,
+                    uint32_t hint_den, esp_extension *out, uint32_t *cigar,
+                    uint32_t cigar_cap);
+
+/* run_band (extend.rs:606-851) with an explicit band, exposed for kernel
+ * equivalence checks the way the reference's own tests call it.  half < 0
+ * selects the full matrix (band_spec None). */
+int esp_run_band(esp_handle *h, const uint8_t *read, size_t read_len, const uint8_t *ref_window,
+                 size_t window_len, const esp_extend_params *params, int64_t band_offset,
+                 int64_t band_half, esp_extension *out, uint32_t *cigar, uint32_t cigar_cap);
+
+/* ---- batch API (new; beside the per-call drop-in) ----
+ *
+ * A batch is a set of read x window pairs whose bases live in one 2-bit
+ * packed arena (MSB-first within each byte, the reference's contig layout,
+ * crates/map/src/fasta.rs:1-5).  Positions are in bases.  Bases that are
+ * not A/C/G/T are listed as half-open N intervals relative to the start of
+ * their sequence (the reference keeps contig N runs the same way). */
+typedef struct {
+    uint64_t read_pos;   /* base offset of the read in the arena              */
+    uint64_t win_pos;    /* base offset of the window in the arena            */
+    uint32_t read_len;
+    uint32_t win_len;
+    int32_t band_offset; /* DiagHint.offset (band centre j - i)               */
+    int32_t band_half;   /* run_band half-width; < 0 = full matrix            */
+    uint32_t n_first;    /* first N interval of this pair                     */
+    uint16_t n_read;     /* N intervals of the read (relative to read start)  */
+    uint16_t n_win;      /* then N intervals of the window                    */
+} esp_pair;
+
+typedef struct {
+    uint32_t start;
+    uint32_t end;
+} esp_n_interval;
+
+#define ESP_MODE_BAND 0 /* run_band with each pair's band (or full matrix)       */
+#define ESP_MODE_HINT 1 /* extend_hint policy with each pair's band_offset       */
+
+/* Upper bounds over a device-resident batch, used to size DP scratch
+ * (pairs beyond them are refused per pair with status ESP_EINVAL). */
+typedef struct {
+    uint32_t max_read_len;
+    uint32_t max_win_len;
+    int32_t max_half;  /* largest band_half; < 0 when any pair runs the full matrix */
+} esp_batch_limits;
+
+/* Device-resident batch: every pointer is device memory; the call is
+ * asynchronous on `stream` (NULL = handle stream).  `cigar` holds
+ * n_pairs * cigar_stride ops.  Returns after enqueueing. */
+int esp_batch_extend_device(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
+                            const uint8_t *arena, uint64_t arena_bytes,
+                            const esp_n_interval *n_iv, uint64_t n_iv_count,
+                            const esp_batch_limits *limits, const esp_extend_params *params,
+                            esp_extension *out, uint32_t *cigar, uint32_t cigar_stride,
+                            void *stream);
+
+/* Host-resident batch: copies inputs to the device, runs, copies results
+ * back and synchronises (the end-to-end path). */
+int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
+                          const uint8_t *arena, uint64_t arena_bytes,
+                          const esp_n_interval *n_iv, uint64_t n_iv_count,
+                          const esp_extend_params *params, esp_extension *out,
+                          uint32_t *cigar, uint32_t cigar_stride);
+
+/* ---- seeded synthetic workloads (the reference ships no datasets) ---- */
+
+/* Arena bytes (16 bytes of padding included) of a Gotoh workload:
+ * config 0 = 150-bp reads vs 214-bp windows, band half 32 at offset 32;
+ * config 2 = read length U[50,300], half in {16,32,64,128} w.p.
+ * {.4,.3,.2,.1}, window read + 2*half, offset half.  Error model: 1%
+ * substitutions, 0.1% indels of length 1-3, A->G at 5% of A (T->C on
+ * reverse-strand pairs). */
+int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int config, uint64_t *arena_bytes);
+/* Fill the workload into caller memory (host). */
+int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
+                    uint64_t arena_bytes, esp_pair *pairs);
+
+/* Number of device kernel launches the last batch call enqueued. */
+uint64_t esp_last_launch_count(const esp_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

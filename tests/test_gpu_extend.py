@@ -1,0 +1,163 @@
+"""GPU parity for the Gotoh DP: the sm_103a kernels against the reference's
+known answers and against the oracle on the reference's seeded sweeps."""
+import numpy as np
+import pytest
+
+import oracle as O
+import refgen as R
+from golden_check import check_extension, load
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import esperanto_gb300 as E  # noqa: E402
+from esperanto_gb300 import batch as B  # noqa: E402
+from gpu_helpers import compare  # noqa: E402
+
+
+def _gpu_kind(kind, case):
+    p = E.ExtendParams(**case["params"])
+    band = tuple(case["band"]) if case.get("band") is not None else None
+    r, w = case["read"], case["window"]
+    if kind in ("run_band_i16", "run_band_i32", "run_dispatch"):
+        return E.run_band(r, w, p, band=band)[0]
+    if kind == "extend":
+        return E.extend(r, w, p)
+    if kind == "extend_hint":
+        return E.extend_hint(r, w, p, hint=E.DiagHint(case.get("offset", 0)))
+    raise AssertionError(kind)
+
+
+def test_known_answers_per_call():
+    G = load()
+    for case in G["extension"]:
+        for kind in case["kinds"]:
+            check_extension(_gpu_kind(kind, case), case["expect"], f"{case['name']} [{kind}]")
+
+
+def test_sweep_band_block_boundaries():
+    cases, dirs, ctx = [], [], []
+    for read, win, d, off, half, c in R.sweep_band_block_boundaries():
+        cases.append((read, win, (off, half)))
+        dirs.append(d)
+        ctx.append(c)
+    assert compare(cases, dirs, ctxs=ctx) > 3000
+
+
+def test_sweep_band():
+    cases, dirs, ctx = [], [], []
+    for read, win, d, off, half, c in R.sweep_band():
+        if len(win) > 2000:
+            continue  # long windows run in their own test
+        cases.append((read, win, (off, half)))
+        dirs.append(d)
+        ctx.append(c)
+    assert compare(cases, dirs, ctxs=ctx) > 400
+
+
+def test_sweep_full_block_boundaries():
+    cases, dirs, ctx = [], [], []
+    for read, win, d, c in R.sweep_full_block_boundaries():
+        cases.append((read, win, None))
+        dirs.append(d)
+        ctx.append(c)
+    compare(cases, dirs, ctxs=ctx)
+
+
+def test_sweep_full_matrix():
+    cases, dirs, ctx = [], [], []
+    for read, win, d, c in R.sweep_full_matrix():
+        if len(win) > 3000:
+            continue
+        cases.append((read, win, None))
+        dirs.append(d)
+        ctx.append(c)
+    assert compare(cases, dirs, ctxs=ctx) > 300
+
+
+def test_long_windows_20000():
+    # n = 20,000 (the documented maximum window, extend.rs:2612-2622, :2793-2821)
+    cases, dirs = [], []
+    for read, win, d, c in R.sweep_full_matrix():
+        if len(win) == 20000:
+            cases.append((read, win, None))
+            dirs.append(d)
+    for read, win, d, off, half, c in R.sweep_band():
+        if len(win) == 20000:
+            cases.append((read, win, (off, half)))
+            dirs.append(d)
+    compare(cases, dirs)
+
+
+def test_hint_policy_sweep():
+    rng = R.Rng(0x5151)
+    cases, dirs = [], []
+    for m, n in [(8, 9), (20, 29), (20, 31), (60, 120), (150, 214), (150, 400), (100, 30)]:
+        for rep in range(6):
+            read = R.rand_seq(rng, m)
+            win = R.rand_window(rng, read, n) if rep % 2 == 0 else R.rand_seq(rng, n)
+            off = rng.below(n + 20) - 10
+            cases.append((read, win, (off, 30)))
+            dirs.append(rep % 3)
+    compare(cases, dirs, mode=B.MODE_HINT)
+
+
+def test_config0_subset_band_and_hint():
+    arena, pairs = B.synth_gotoh(1, 2048, 0)
+    cases = []
+    for k in range(len(pairs)):
+        r, w = B.decode_pair(arena, pairs[k])
+        cases.append((r, w, (int(pairs[k]["band_offset"]), int(pairs[k]["band_half"]))))
+    compare(cases, [0] * len(cases))
+    compare(cases, [0] * len(cases), mode=B.MODE_HINT)
+
+
+def test_config2_subset():
+    arena, pairs = B.synth_gotoh(3, 1024, 2)
+    cases = []
+    for k in range(len(pairs)):
+        r, w = B.decode_pair(arena, pairs[k])
+        cases.append((r, w, (int(pairs[k]["band_offset"]), int(pairs[k]["band_half"]))))
+    compare(cases, [1] * len(cases))
+
+
+def test_batch_direct_synth_matches_oracle_batch():
+    # the synthetic arena straight into the batch API (no ASCII round trip)
+    arena, pairs = B.synth_gotoh(11, 4096, 0)
+    out, cig = B.extend_batch_host(pairs, arena, params=E.ExtendParams(), mode=B.MODE_BAND,
+                                   cigar_stride=32)
+    assert (out["status"] == 0).all()
+    for k in range(0, len(pairs), 97):
+        r, w = B.decode_pair(arena, pairs[k])
+        want = O.run_dispatch(r, w, O.Params(), band=(32, 32))[0].key()
+        got = (int(out[k]["score"]), int(out[k]["read_start"]), int(out[k]["read_end"]),
+               int(out[k]["ref_start"]), tuple(B.cigar_of(cig[k], int(out[k]["n_ops"]))))
+        assert got == want
+
+
+def test_empty_and_degenerate_inputs():
+    assert E.run_band(b"", b"ACGT")[0].key() == (0, 0, 0, 0, ())
+    assert E.run_band(b"ACGT", b"")[0].key() == (0, 0, 0, 0, (("S", 4),))
+    assert E.extend_hint(b"ACGT", b"").key() == (0, 0, 0, 0, (("S", 4),))
+    # all-N read: score 0, whole-read soft clip
+    assert E.extend(b"NNNN", b"ACGT").key() == O.extend(b"NNNN", b"ACGT").key()
+
+
+def test_cigar_capacity_reported():
+    read = b"ACGT" * 10
+    win = b"ACGA" * 10
+    with pytest.raises(E.EspError):
+        import ctypes as C
+        from esperanto_gb300 import _native as N
+        buf = E.extend._default_buffer() if hasattr(E.extend, "_default_buffer") else None
+        from esperanto_gb300.extend import _default_buffer
+        buf = _default_buffer()
+        p = E.ExtendParams()._c()
+        out = N.ExtensionC()
+        ops = (C.c_uint32 * 1)()
+        rc = N.lib().esp_extend(buf.handle, read, len(read), win, len(win), C.byref(p),
+                                C.byref(out), ops, 1)
+        buf.check(rc)
