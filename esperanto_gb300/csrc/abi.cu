@@ -32,6 +32,11 @@ struct esp_handle {
     uint32_t *d_esc = nullptr;  // escalation list
     size_t d_esc_cap = 0;       // bytes
     uint32_t *d_ctr = nullptr;  // [0..1] queues (u64), [4] esc count
+    uint32_t *d_hist = nullptr; // geometry bins
+    size_t d_hist_cap = 0;
+    uint32_t *d_order = nullptr;  // length-binned work list
+    size_t d_order_cap = 0;
+    bool binning = true;
     // host pinned staging
     void *h_in = nullptr;
     size_t h_in_cap = 0;
@@ -162,7 +167,19 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
         return rc;
     CK(h, cudaMemsetAsync(h->d_ctr, 0, 64, st));
+    const uint32_t *order = nullptr;
+    if (h->binning && n_pairs > 32) {
+        if ((rc = grow_device(h, (void **)&h->d_hist, &h->d_hist_cap, esp::bin_scratch_bytes())) != ESP_OK)
+            return rc;
+        if ((rc = grow_device(h, (void **)&h->d_order, &h->d_order_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
+            return rc;
+        CK(h, esp::launch_binning(d_pairs, n_pairs, mode == ESP_MODE_HINT ? 1 : 0, h->d_hist,
+                                  h->d_order, h->num_sms, st));
+        h->launches += 3;
+        order = h->d_order;
+    }
     esp::GotohJob job{};
+    job.list = order;
     job.pairs = d_pairs;
     job.n_pairs = n_pairs;
     job.arena = d_arena;
@@ -186,6 +203,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     if (mode == ESP_MODE_HINT) {
         esp::GotohJob j2 = job;
         j2.mode = 2;
+        j2.list_count = nullptr;
         j2.list = h->d_esc;
         j2.list_count = h->d_ctr + 4;
         j2.queue = h->d_ctr + 2;
@@ -228,6 +246,8 @@ int esp_destroy(esp_handle *h) {
     cudaFree(h->d_esc);
     cudaFree(h->d_ctr);
     cudaFree(h->d_bat);
+    cudaFree(h->d_hist);
+    cudaFree(h->d_order);
     if (h->h_in) cudaFreeHost(h->h_in);
     if (h->h_res) cudaFreeHost(h->h_res);
     if (h->stream) cudaStreamDestroy(h->stream);

@@ -60,6 +60,12 @@ cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, in
 // Resident blocks per SM of the DP kernel at `block` threads.
 int gotoh_blocks_per_sm(int block);
 
+// Counting-sort the pairs by geometry (descending cost) into `order`.
+// `hist` needs bin_scratch_bytes() of device memory.  4 launches.
+cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
+                           uint32_t *order, int num_sms, cudaStream_t st);
+size_t bin_scratch_bytes();
+
 // Traceback and row-buffer words one thread needs for a pair.
 void gotoh_scratch_words(uint32_t m, uint32_t n, int32_t half, uint64_t &tb, uint64_t &rb);
 
