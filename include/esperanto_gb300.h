@@ -39,6 +39,7 @@ extern "C" {
 #define ESP_EBUSY (-6)    /* admission refused (serve loop over budget)      */
 #define ESP_ETIMEOUT (-7) /* bounded wait expired                            */
 #define ESP_ECLOSED (-8)  /* queue closed                                    */
+#define ESP_ESCRATCH (-9) /* work too large for the fixed no-allocation scratch */
 
 #define ESP_OP_M 0
 #define ESP_OP_I 1
@@ -165,6 +166,37 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
                           const esp_n_interval *n_iv, uint64_t n_iv_count,
                           const esp_extend_params *params, esp_extension *out,
                           uint32_t *cigar, uint32_t cigar_stride);
+
+/* ---- allocation-free variant (no counterpart in the reference) ----
+ *
+ * esp_batch_run_band_noalloc: the same banded/full-matrix DP with traceback
+ * as esp_batch_extend_device in ESP_MODE_BAND, for callers that must not
+ * allocate device memory after start-up -- a host runtime that owns all
+ * device memory through its own pre-sized pool, or a latency-bound request
+ * path that cannot afford cudaMalloc/cudaFree (which can synchronise the
+ * whole device).  It calls no cudaMalloc, cudaFree or other allocating
+ * routine and needs no handle: its scratch is one fixed array of
+ * ESP_NOALLOC_SCRATCH_BYTES in device memory, held by every GPU that loads
+ * this library until the process exits.
+ *   - Inputs and outputs are caller-owned device memory, as for
+ *     esp_batch_extend_device; the call is asynchronous on `stream`
+ *     (NULL = legacy default stream) on the current device.
+ *   - The first call on a device looks up the array's device address for
+ *     that device; make that first call before any stream capture.
+ *   - Every call shares the one array: calls that can overlap on the GPU
+ *     (different streams, different host threads) race and must be
+ *     serialised by the caller.
+ *   - Work whose per-block scratch (4 warps x 32 pairs of traceback and
+ *     row-buffer words, sized from `limits`) exceeds the array returns
+ *     ESP_ESCRATCH; smaller work runs with fewer resident blocks when the
+ *     array cannot hold a full persistent grid.
+ *   - Pairs run in the order given (no length binning). */
+#define ESP_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int esp_batch_run_band_noalloc(const esp_pair *pairs, uint64_t n_pairs, const uint8_t *arena,
+                               uint64_t arena_bytes, const esp_n_interval *n_iv,
+                               uint64_t n_iv_count, const esp_batch_limits *limits,
+                               const esp_extend_params *params, esp_extension *out,
+                               uint32_t *cigar, uint32_t cigar_stride, void *stream);
 
 /* ---- seeded synthetic workloads (the reference ships no datasets) ---- */
 
