@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -18,7 +19,8 @@ struct esp_handle {
     cudaStream_t stream = nullptr;
     std::string err;
     uint64_t launches = 0;
-    int gotoh_bps = 0;  // resident DP blocks per SM (queried once)
+    int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
+    int variant = -1;   // DP kernel variant; -1 = ESP_GOTOH_VARIANT env or default
     uint64_t scratch_budget = 8ull << 30;  // bytes of DP scratch one launch may use
     // grow-only device buffers
     void *d_in = nullptr;       // per-call staging: pair | n intervals | arena
@@ -152,8 +154,13 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
     uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
     uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    if (h->gotoh_bps == 0) h->gotoh_bps = esp::gotoh_blocks_per_sm(128);
-    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * h->gotoh_bps * 4);
+    if (h->variant < 0) {
+        const char *v = getenv("ESP_GOTOH_VARIANT");
+        h->variant = (v && *v == '0') ? 0 : 1;
+    }
+    const int var = h->variant;
+    if (h->gotoh_bps[var] == 0) h->gotoh_bps[var] = esp::gotoh_blocks_per_sm(128, var);
+    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * h->gotoh_bps[var] * 4);
     uint64_t need_warps = (n_pairs + 31) / 32;
     uint64_t warps = std::min(want, need_warps);
     uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes);
@@ -198,7 +205,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     job.esc_count = h->d_ctr + 4;
     job.mode = mode == ESP_MODE_HINT ? 1 : 0;
     job.max_m = (int)L1.max_m;
-    CK(h, esp::launch_gotoh(job, K, (int)warps, 128, st));
+    CK(h, esp::launch_gotoh(job, K, (int)warps, 128, st, var));
     h->launches++;
     if (mode == ESP_MODE_HINT) {
         esp::GotohJob j2 = job;
@@ -207,7 +214,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         j2.list = h->d_esc;
         j2.list_count = h->d_ctr + 4;
         j2.queue = h->d_ctr + 2;
-        CK(h, esp::launch_gotoh(j2, K, (int)warps, 128, st));
+        CK(h, esp::launch_gotoh(j2, K, (int)warps, 128, st, var));
         h->launches++;
     }
     return ESP_OK;

@@ -54,11 +54,13 @@ struct GotohJob {
 };
 
 // Launch the persistent DP kernel with `warps` warps total.
+// variant 0: 3 resident 128-thread blocks per SM (168 registers); 1: 4 blocks.
 cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, int block,
-                         cudaStream_t st);
+                         cudaStream_t st, int variant);
+constexpr int kGotohVariants = 2;
 
 // Resident blocks per SM of the DP kernel at `block` threads.
-int gotoh_blocks_per_sm(int block);
+int gotoh_blocks_per_sm(int block, int variant);
 
 // Counting-sort the pairs by geometry (descending cost) into `order`.
 // `hist` needs bin_scratch_bytes() of device memory.  4 launches.

@@ -76,38 +76,47 @@ struct Strip {
     int lo[STRIP], hi[STRIP];
 };
 
+__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;  // integer multiply-add: issues on the FMA pipe, off the saturated ALU pipe
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // One column of one strip.  upH/upE enter as the row above the strip at
 // column j and leave as the strip's last row at column j; `diag` is the row
-// above at column j-1.  Returns the column's packed traceback word.
-template <bool MASKED>
+// above at column j-1; cj = 32767 - j (row-max key tie order).  MASK = 1
+// tests every cell against its row window (strip ramps); MASK = 0 is the
+// strip interior where all 8 cells are in window.
+template <int MASK>
 __device__ __forceinline__ uint32_t dp_column(Strip &S, const GotohConst &K, int j, uint32_t sel,
-                                              int cj, int &upH, int &upE, int diag) {
+                                              uint32_t cj, int &upH, int &upE, int diag) {
     uint32_t wa = 0, wb = 0;
     int d = diag;
 #pragma unroll
     for (int r = 0; r < STRIP; r++) {
         int left = S.Hl[r];
-        int kE = max(upH + K.oe1, upE + K.ex4);
-        int kF = max(left + K.oe4, S.Fl[r] + K.ex4);
+        int kE = max(upE + K.ex4, upH + K.oe1);
+        int kF = max(S.Fl[r] + K.ex4, left + K.oe4);
         int E4 = kE & ~3;
         int F4 = kF & ~3;
-        int kd = d + prmt_sx(S.l0[r], S.l1[r], sel);
-        int key = max(max(kd, kE | 1), max(F4, 3));
+        int kd = max(d + prmt_sx(S.l0[r], S.l1[r], sel), 3);  // START tag 3 folded in
+        int key = max(max(kd, kE | 1), F4);
         int Hp = (key & ~3) | 2;
-        wa = (wa << 2) | (uint32_t)(key & 3);
-        wb = (wb << 2) | (uint32_t)((kE & 1) | (kF & 2));
-        if (MASKED) {
+        wa = mad_u32(wa, 4u, (uint32_t)(key & 3));
+        wb = mad_u32(wb, 4u, (uint32_t)((kE & 1) | (kF & 2)));
+        int rkey = (int)mad_u32((uint32_t)Hp, 32768u, cj);
+        if (MASK) {
             bool in = (j >= S.lo[r]) & (j <= S.hi[r]);
             if (j == S.hi[r]) S.hr[r] = Hp;
             if (in) {
-                S.rk[r] = max(S.rk[r], (Hp << 15) + cj);
+                S.rk[r] = max(S.rk[r], rkey);
             } else {
                 Hp = 2;
                 E4 = NEG4;
                 F4 = NEG4;
             }
         } else {
-            S.rk[r] = max(S.rk[r], (Hp << 15) + cj);
+            S.rk[r] = max(S.rk[r], rkey);
         }
         d = left;
         S.Hl[r] = Hp;
@@ -124,40 +133,56 @@ struct FillResult {
     bool tleft, tclamp;
 };
 
-// Column range [a, b] of a strip, MASKED or not.
-template <bool MASKED>
-__device__ __forceinline__ void dp_range(Strip &S, const GotohConst &K, int a, int b, int &diag,
-                                         uint32_t &cw, uint32_t &nm, int &kk, const Seq &win,
-                                         const uint32_t *rb, int plo, int phi, bool have_prev,
-                                         uint32_t *rbw, int lo7, bool write_rb, uint32_t *tbp,
-                                         int clo) {
-    for (int j = a; j <= b; j++) {
-        if (kk == 16) {
-            cw = load16(win.arena, win.pos + (uint64_t)(j - 1));
-            nm = win.cnt ? nmask16(win.iv, win.cnt, j - 1) : 0u;
-            kk = 0;
+// Columns [a, b] of the current strip.  Window codes are fetched 16 at a
+// time.  CHECK = true (strip ramps) tests the row-buffer read (the row above
+// has a value only up to phi) and write (the strip's last row starts at
+// lo7) per column; the interior needs neither test.
+template <int MASK, bool CHECK, bool HASN>
+__device__ __forceinline__ void dp_cols(Strip &S, const GotohConst &K, int a, int b, int &diag,
+                                        const Seq &win, uint32_t *rb, int plo, int phi, int lo7,
+                                        uint32_t *tbp) {
+    uint32_t *rbr = rb + (size_t)(a - plo) * 32;
+    uint32_t cj = 32767u - (uint32_t)a;
+    for (int j = a; j <= b;) {
+        uint32_t cw = load16(win.arena, win.pos + (uint64_t)(j - 1));
+        uint32_t nm = HASN ? nmask16(win.iv, win.cnt, j - 1) : 0u;
+        int cnt = min(16, b - j + 1);
+#pragma unroll 2
+        for (int k = 0; k < cnt; k++, j++) {
+            uint32_t code = HASN ? ((cw >> 30) | ((nm >> 29) & 4u)) : (cw >> 30);
+            cw <<= 2;
+            if (HASN) nm <<= 1;
+            uint32_t sel = code * 0x1111u + 0x8880u;
+            int bH = 2, bE = NEG4;
+            if (!CHECK || j <= phi) {
+                uint32_t w = *rbr;
+                bH = (int)(w & 0xffffu);
+                bE = ((int)w) >> 16;
+            }
+            int upH = bH, upE = bE;
+            uint32_t word = dp_column<MASK>(S, K, j, sel, cj, upH, upE, diag);
+            diag = bH;
+            uint32_t packed = __byte_perm((uint32_t)upH, (uint32_t)upE, 0x5410);
+            if (CHECK) {
+                if (j >= lo7) rb[(size_t)(j - lo7) * 32] = packed;
+            } else {
+                rbr[(ptrdiff_t)(plo - lo7) * 32] = packed;  // row-buffer slot j - lo7
+            }
+            *tbp = word;
+            tbp += 32;
+            rbr += 32;
+            cj--;
         }
-        uint32_t code = (cw >> 30) | ((nm >> 29) & 4u);
-        cw <<= 2;
-        nm <<= 1;
-        kk++;
-        uint32_t sel = code * 0x1111u + 0x8880u;
-        int bH = 2, bE = NEG4;
-        if (have_prev && j <= phi) {
-            uint32_t w = rb[(size_t)(j - plo) * 32];
-            bH = (int)(w & 0xffffu);
-            bE = ((int)w) >> 16;
-        }
-        int upH = bH, upE = bE;
-        uint32_t word = dp_column<MASKED>(S, K, j, sel, 32767 - j, upH, upE, diag);
-        diag = bH;
-        if (write_rb && j >= lo7)
-            rbw[(size_t)(j - lo7) * 32] = __byte_perm((uint32_t)upH, (uint32_t)upE, 0x5410);
-        tbp[(size_t)(j - clo) * 32] = word;
     }
 }
 
 // Fill the DP for one pair; traceback words land in tb (stride sw per strip).
+// The row buffer holds sw words: strip 0 reads row 0 (H = 0, E = NEG on every
+// column, extend.rs:664-681) from a prefilled copy, later strips read the last
+// row of the previous strip, which each strip rewrites in place (a slot is
+// always read at or before the column that overwrites it, since the strip's
+// window start lo7 never precedes the previous row's start plo).
+template <bool HASN>
 __device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ s_lut, int m,
                               int n, const Geo &g, const Seq &read, const Seq &win,
                               uint32_t *tb, int sw, uint32_t *rb) {
@@ -169,7 +194,11 @@ __device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ 
     R.tleft = false;
     R.tclamp = false;
     int nstrips = (m + STRIP - 1) / STRIP;
-    int plo = 0, phi = -1;
+    int plo = g.lo(1), phi = g.hi(min(STRIP, m));
+    {
+        const uint32_t row0 = __byte_perm(2u, (uint32_t)NEG4, 0x5410);
+        for (int k = 0; k <= phi - plo; k++) rb[(size_t)k * 32] = row0;
+    }
     Strip S;
     for (int s = 0; s < nstrips; s++) {
         int i0 = s * STRIP + 1;
@@ -197,23 +226,20 @@ __device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ 
             S.l0[r] = s_lut[2 * c];
             S.l1[r] = s_lut[2 * c + 1];
         }
-        bool have_prev = s > 0;
         int diag = 2;
-        if (have_prev && clo - 1 >= plo && clo - 1 <= phi)
+        if (clo - 1 >= plo && clo - 1 <= phi)
             diag = (int)(rb[(size_t)(clo - 1 - plo) * 32] & 0xffffu);
-        uint32_t cw = 0, nm = 0;
-        int kk = 16;
-        bool write_rb = s + 1 < nstrips;
         uint32_t *tbp = tb + (size_t)s * sw * 32;
         int a_end = min(lo7, chi);
-        dp_range<true>(S, K, clo, a_end, diag, cw, nm, kk, win, rb, plo, phi, have_prev, rb, lo7,
-                       write_rb, tbp, clo);
-        int b_end = min(hi0 - 1, chi);
-        dp_range<false>(S, K, lo7 + 1, b_end, diag, cw, nm, kk, win, rb, plo, phi, have_prev, rb,
-                        lo7, write_rb, tbp, clo);
+        dp_cols<1, true, HASN>(S, K, clo, a_end, diag, win, rb, plo, phi, lo7, tbp);
+        int b_beg = lo7 + 1, b_end = min(hi0 - 1, chi);
+        if (b_beg <= b_end)
+            dp_cols<0, false, HASN>(S, K, b_beg, b_end, diag, win, rb, plo, phi, lo7,
+                                    tbp + (size_t)(b_beg - clo) * 32);
         int c_beg = max(lo7 + 1, hi0);
-        dp_range<true>(S, K, c_beg, chi, diag, cw, nm, kk, win, rb, plo, phi, have_prev, rb, lo7,
-                       write_rb, tbp, clo);
+        if (c_beg <= chi)
+            dp_cols<1, true, HASN>(S, K, c_beg, chi, diag, win, rb, plo, phi, lo7,
+                                   tbp + (size_t)(c_beg - clo) * 32);
         // row bookkeeping in row order (extend.rs:795-827)
 #pragma unroll
         for (int r = 0; r < STRIP; r++) {
@@ -248,62 +274,126 @@ __device__ __forceinline__ bool neutral_col(uint32_t q, uint32_t r) {
     return q < 4 && r < 4 && (q == r || (r == 0 && q == 2) || (r == 3 && q == 1));
 }
 
-// One traceback step from (i, j) in `state` (0 H, 1 E, 2 F).  Returns false
-// when the walk stops (extend.rs:884-930).
-struct Step {
-    int op, d;
-};
+// Step kinds recorded by the first traceback walk (4 bits each) so the second
+// walk replays from registers/local memory instead of re-reading the
+// traceback words: M with a match / mismatch / zero (editing-exempt) score,
+// I or D opening a gap run (walk order), I or D extending it.
+enum : int { K_MM = 0, K_MX = 1, K_MZ = 2, K_IO = 3, K_IE = 4, K_DO = 5, K_DE = 6 };
+constexpr int REC_WORDS = 64;  // 512 recorded steps; longer walks re-walk
 
-__device__ __forceinline__ bool tb_step(const GotohConst &K, const int8_t *__restrict__ lut,
-                                        const Geo &g, const uint32_t *tb, int sw, const Seq &read,
-                                        const Seq &win, int &i, int &j, int &state, Step &st) {
-    if (i <= 0 || j <= 0) return false;
-    if (j < g.lo(i) || j > g.hi(i)) return false;
-    int s = (i - 1) >> 3, r = (i - 1) & 7;
-    int clo = g.lo(s * STRIP + 1);
-    uint32_t w = tb[((size_t)s * sw + (size_t)(j - clo)) * 32];
-    int sh = 2 * (7 - r);
-    uint32_t hsrc = (w >> sh) & 3u;
-    uint32_t eo = (w >> (16 + sh)) & 1u;
-    uint32_t fo = (w >> (17 + sh)) & 1u;
-    if (state == 0) {
-        if (hsrc == 2u) {
-            uint32_t q = read.code(i - 1), rc = win.code(j - 1);
-            st.op = ESP_OP_M;
-            st.d = lut[q * 5 + rc];
-            i--;
-            j--;
-        } else if (hsrc == 1u) {
-            st.op = ESP_OP_I;
-            st.d = K.open_ext;
-            state = eo ? 0 : 1;
-            i--;
-        } else if (hsrc == 0u) {
-            st.op = ESP_OP_D;
-            st.d = K.open_ext;
-            state = fo ? 0 : 2;
-            j--;
-        } else {
-            return false;  // H_START
+__device__ __forceinline__ int kind_op(int k) { return k < 3 ? ESP_OP_M : (k < 5 ? ESP_OP_I : ESP_OP_D); }
+
+// One traceback walk over the packed bits (extend.rs:884-930): state machine
+// H/E/F from (best_i, best_j), stopping at i <= 0, j <= 0, outside the row
+// window, or on an H START cell.  Word loads are cached and the word of the
+// next column is prefetched (most steps move one column left in the strip);
+// read and window codes are cached 16 bases at a time.
+struct Walker {
+    const Geo &g;
+    const uint32_t *tb;
+    int sw;
+    const Seq &read;
+    const Seq &win;
+    const GotohConst &K;
+    int i, j, state;
+    int cs, cclo;          // current strip and its first column
+    int64_t ck, nk;        // cached / prefetched word index
+    uint32_t cw, nw;
+    int64_t rq, wq;        // first position of the cached code words
+    uint32_t rword, rnm, wword, wnm;
+
+    __device__ Walker(const Geo &g_, const uint32_t *tb_, int sw_, const Seq &r_, const Seq &w_,
+                      const GotohConst &K_, int bi, int bj)
+        : g(g_), tb(tb_), sw(sw_), read(r_), win(w_), K(K_), i(bi), j(bj), state(0), cs(-1),
+          cclo(0), ck(-1), nk(-1), cw(0), nw(0), rq(-100), wq(-100), rword(0), rnm(0), wword(0),
+          wnm(0) {}
+
+    __device__ __forceinline__ uint32_t rcode(int64_t q) {
+        if (q < rq || q >= rq + 16) {
+            rq = q >= 15 ? q - 15 : 0;
+            rword = load16(read.arena, read.pos + (uint64_t)rq);
+            rnm = read.cnt ? nmask16(read.iv, read.cnt, rq) : 0u;
         }
-    } else if (state == 1) {
-        st.op = ESP_OP_I;
-        st.d = K.ext;
-        if (eo) state = 0;
-        i--;
-    } else {
-        st.op = ESP_OP_D;
-        st.d = K.ext;
-        if (fo) state = 0;
-        j--;
+        int k = (int)(q - rq);
+        return ((rnm >> (31 - k)) & 1u) ? 4u : ((rword >> (30 - 2 * k)) & 3u);
     }
-    return true;
-}
+    __device__ __forceinline__ uint32_t wcode(int64_t q) {
+        if (q < wq || q >= wq + 16) {
+            wq = q >= 15 ? q - 15 : 0;
+            wword = load16(win.arena, win.pos + (uint64_t)wq);
+            wnm = win.cnt ? nmask16(win.iv, win.cnt, wq) : 0u;
+        }
+        int k = (int)(q - wq);
+        return ((wnm >> (31 - k)) & 1u) ? 4u : ((wword >> (30 - 2 * k)) & 3u);
+    }
+
+    // Take one step; returns false when the walk stops.  `kind` is the step.
+    __device__ __forceinline__ bool step(int &kind) {
+        if (i <= 0 || j <= 0) return false;
+        if (j < g.lo(i) || j > g.hi(i)) return false;
+        int s = (i - 1) >> 3, r = (i - 1) & 7;
+        if (s != cs) {
+            cs = s;
+            cclo = g.lo(s * STRIP + 1);
+        }
+        int64_t idx = (int64_t)s * sw + (j - cclo);
+        uint32_t w;
+        if (idx == ck) {
+            w = cw;
+        } else if (idx == nk) {
+            w = nw;
+        } else {
+            w = tb[(size_t)idx * 32];
+        }
+        ck = idx;
+        cw = w;
+        if (j - 1 >= cclo) {  // prefetch the word one column left (same strip)
+            nk = idx - 1;
+            nw = tb[(size_t)nk * 32];
+        } else {
+            nk = -1;
+        }
+        int sh = 2 * (7 - r);
+        uint32_t hsrc = (w >> sh) & 3u;
+        uint32_t eo = (w >> (16 + sh)) & 1u;
+        uint32_t fo = (w >> (17 + sh)) & 1u;
+        if (state == 0) {
+            if (hsrc == 2u) {
+                uint32_t q = rcode(i - 1), rc = wcode(j - 1);
+                if (q == rc && q < 4) kind = K_MM;
+                else if ((K.edit_dir == ESP_EDIT_AG && q == 2 && rc == 0) ||
+                         (K.edit_dir == ESP_EDIT_TC && q == 1 && rc == 3))
+                    kind = K_MZ;
+                else kind = K_MX;
+                i--;
+                j--;
+            } else if (hsrc == 1u) {
+                kind = K_IO;
+                state = eo ? 0 : 1;
+                i--;
+            } else if (hsrc == 0u) {
+                kind = K_DO;
+                state = fo ? 0 : 2;
+                j--;
+            } else {
+                return false;  // H_START
+            }
+        } else if (state == 1) {
+            kind = K_IE;
+            if (eo) state = 0;
+            i--;
+        } else {
+            kind = K_DE;
+            if (fo) state = 0;
+            j--;
+        }
+        return true;
+    }
+};
 
 struct CigarOut {
     uint32_t *p;
     uint32_t cap;
-    uint32_t n;
     bool overflow;
     __device__ __forceinline__ void put(uint32_t idx, uint32_t v) {
         if (idx < cap) p[idx] = v;
@@ -316,21 +406,31 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
                           const uint32_t *tb, int sw, int m, int n, const Seq &read,
                           const Seq &win, const FillResult &F, esp_extension &o, uint32_t *cig,
                           uint32_t cap) {
-    // walk 1: number of steps N, total T, trail
+    const int dtab[7] = {K.match, (int)K.lut[1], 0, K.open_ext, K.ext, K.open_ext, K.ext};
+    uint32_t rec[REC_WORDS];
+    // walk 1: number of steps N, total T, trail; steps recorded for walk 2
     int N = 0, P = 0, trail = 0;
     {
-        int i = F.best_i, j = F.best_j, state = 0;
-        Step st;
-        while (tb_step(K, lut, g, tb, sw, read, win, i, j, state, st)) {
-            P += st.d;
+        Walker W(g, tb, sw, read, win, K, F.best_i, F.best_j);
+        int kind;
+        uint32_t acc = 0;
+        while (W.step(kind)) {
+            P += dtab[kind];
+            acc |= (uint32_t)kind << (4 * (N & 7));
             N++;
+            if ((N & 7) == 0) {
+                if ((N >> 3) <= REC_WORDS) rec[(N >> 3) - 1] = acc;
+                acc = 0;
+            }
             if (P <= 0) trail = N;
         }
+        if ((N & 7) && (N >> 3) < REC_WORDS) rec[N >> 3] = acc;
     }
+    const bool replay = N <= REC_WORDS * 8;
     const int T = P;
     uint32_t read_start, ref_start, read_end, ref_end;
     int score = 0;
-    CigarOut co{cig, cap, 0, false};
+    CigarOut co{cig, cap, false};
     uint32_t K_runs = 0;  // kept runs, written from index 2 in walk order
     int first_op = -1, last_op = -1;  // forward order first / last kept op
     if (N == 0) {
@@ -347,7 +447,8 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
         // middle step) is captured on the way in case that happens.
         bool degenerate = (T <= 0);  // u = -1
         const int tstar = N - 1 - N / 2;
-        int i = F.best_i, j = F.best_j, state = 0;
+        Walker W(g, tb, sw, read, win, K, F.best_i, F.best_j);
+        int i = F.best_i, j = F.best_j;
         int pos_acc = 0;
         bool found = false;
         int cur_op = -1;
@@ -357,17 +458,21 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
         bool done = false;
         for (int t = 0; t < N && !done; t++) {
             int i_before = i, j_before = j;
-            Step st;
-            tb_step(K, lut, g, tb, sw, read, win, i, j, state, st);
+            int kind;
+            if (replay) kind = (int)((rec[t >> 3] >> (4 * (t & 7))) & 15u);
+            else W.step(kind);
+            int op = kind_op(kind), d = dtab[kind];
+            if (op != ESP_OP_D) i--;
+            if (op != ESP_OP_I) j--;
             if (t == tstar) {
                 ts_ib = i_before;
                 ts_jb = j_before;
                 ts_ia = i;
                 ts_ja = j;
-                ts_op = st.op;
-                ts_d = st.d;
+                ts_op = op;
+                ts_d = d;
             }
-            pos_acc += st.d;
+            pos_acc += d;
             if (!degenerate && !found && t <= N - 2 && pos_acc >= T) {
                 found = true;
                 if (t < trail) degenerate = true;  // nothing emitted yet
@@ -380,17 +485,17 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
                 if (t == trail) {
                     read_end = (uint32_t)i_before;
                     ref_end = (uint32_t)j_before;
-                    last_op = st.op;
+                    last_op = op;
                 }
-                score += st.d;
-                if (st.op == cur_op) {
+                score += d;
+                if (op == cur_op) {
                     cur_len++;
                 } else {
                     if (cur_op >= 0) co.put(2 + K_runs++, (cur_len << 4) | (uint32_t)cur_op);
-                    cur_op = st.op;
+                    cur_op = op;
                     cur_len = 1;
                 }
-                first_op = st.op;
+                first_op = op;
                 if (found) {  // t == u_min: the kept region starts here
                     read_start = (uint32_t)i;
                     ref_start = (uint32_t)j;
@@ -524,7 +629,7 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     g.n = n;
     int sw = full ? n : min(2 * g.half + STRIP, n);
     uint64_t need_tb = (uint64_t)((m + STRIP - 1) / STRIP) * (uint64_t)sw;
-    uint64_t need_rb = (uint64_t)min(2 * g.half + 1, n);
+    uint64_t need_rb = (uint64_t)sw;
     if (need_tb > job.tb_words || need_rb > job.rb_words) {
         o.status = ESP_EINVAL;  // scratch sized too small by the host: refuse, never overrun
         job.out[pi] = o;
@@ -540,7 +645,8 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     const esp_n_interval *iv = job.n_iv + P.n_first;
     Seq read{job.arena, P.read_pos, iv, P.n_read};
     Seq win{job.arena, P.win_pos, iv + P.n_read, P.n_win};
-    FillResult F = dp_fill(K, s_lut, m, n, g, read, win, tb, sw, rb);
+    FillResult F = win.cnt ? dp_fill<true>(K, s_lut, m, n, g, read, win, tb, sw, rb)
+                           : dp_fill<false>(K, s_lut, m, n, g, read, win, tb, sw, rb);
     dp_finish(K, lut, g, tb, sw, m, n, read, win, F, o, cig, job.cigar_stride);
     if (F.trow) {
         o.touched = 1;
@@ -560,7 +666,8 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     job.out[pi] = o;
 }
 
-__global__ void __launch_bounds__(128, 4) gotoh_kernel(GotohJob job, GotohConst K) {
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) gotoh_kernel(GotohJob job, GotohConst K) {
     __shared__ uint32_t s_lut[10];
     __shared__ int8_t s_lut25[32];
     if (threadIdx.x == 0) {  // static indices keep the parameter block out of local memory
@@ -627,21 +734,28 @@ void gotoh_scratch_words(uint32_t m, uint32_t n, int32_t half, uint64_t &tb, uin
     int64_t h = full ? n : half;
     int64_t sw = full ? n : (2 * h + STRIP < (int64_t)n ? 2 * h + STRIP : (int64_t)n);
     tb = (uint64_t)((m + STRIP - 1) / STRIP) * (uint64_t)sw;
-    rb = (uint64_t)(2 * h + 1 < (int64_t)n ? 2 * h + 1 : (int64_t)n);
+    rb = (uint64_t)sw;
 }
 
-int gotoh_blocks_per_sm(int block) {
+// Kernel variants: resident blocks per SM requested at compile time.  More
+// blocks mean fewer registers per thread (spills) but more warps to hide
+// latency; which wins depends on the band width, so the host picks per
+// launch (see the tuning in abi.cu).
+int gotoh_blocks_per_sm(int block, int variant) {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel, block, 0) != cudaSuccess)
-        return 1;
+    cudaError_t e = variant == 0
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel<3>, block, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel<4>, block, 0);
+    if (e != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
 
 cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, int block,
-                         cudaStream_t st) {
+                         cudaStream_t st, int variant) {
     int threads = warps * 32;
     int grid = (threads + block - 1) / block;
-    gotoh_kernel<<<grid, block, 0, st>>>(job, k);
+    if (variant == 0) gotoh_kernel<3><<<grid, block, 0, st>>>(job, k);
+    else gotoh_kernel<4><<<grid, block, 0, st>>>(job, k);
     return cudaGetLastError();
 }
 

@@ -53,7 +53,7 @@ int setup_device(int dev) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return ESP_ECUDA;
-    g_blocks_per_sm[dev] = esp::gotoh_blocks_per_sm(128);
+    g_blocks_per_sm[dev] = esp::gotoh_blocks_per_sm(128, 1);
     g_num_sms[dev] = sms;
     g_scratch_addr[dev] = p;
     return ESP_OK;
@@ -119,6 +119,6 @@ extern "C" int esp_batch_run_band_noalloc(const esp_pair *pairs, uint64_t n_pair
     job.rb = job.tb + warps * 32 * tbw;
     job.rb_words = rbw;
     job.max_m = (int)limits->max_read_len;
-    if (esp::launch_gotoh(job, K, (int)warps, 128, st) != cudaSuccess) return ESP_ECUDA;
+    if (esp::launch_gotoh(job, K, (int)warps, 128, st, 1) != cudaSuccess) return ESP_ECUDA;
     return ESP_OK;
 }
