@@ -30,6 +30,8 @@ sys.path.insert(0, ROOT)
 
 OPS_PER_CELL = 21  # integer ops of the cell recurrence as written in gotoh.cu (see DESIGN)
 INT_LANES_PER_SM = 128
+# Myers: 10 32-bit ops per 32-cell limb per text column (wide-word step)
+MYERS_OPS_PER_CELL = 10.0 / 32.0
 
 
 def load_peaks():
@@ -41,6 +43,9 @@ def load_peaks():
 
 
 def workload_desc(config: int, n: int) -> str:
+    if config == 1:
+        return (f"bit-parallel EA-Myers infix_best_end: {n} pairs, 150-bp query vs 200-bp "
+                "text, 0-8 edits, 10% unrelated")
     if config == 0:
         return (f"plain banded Gotoh: {n} pairs, 150-bp reads vs 214-bp windows, "
                 "band half 32 at offset 32, traceback to CIGAR")
@@ -120,6 +125,19 @@ def cpu_reference(args, config, n_pairs, seed, threads):
     import oracle as O
     from esperanto_gb300 import batch as B
     sample = args.cpu_sample
+    if config == 1:
+        sample = sample * 16
+        arena, pairs = B.synth_myers(seed, sample)
+        end = int((pairs["text_pos"] + pairs["text_len"]).max())
+        seq = B._ASCII[B.unpack_codes(arena, 0, end)]
+        O.build()
+
+        def run_m():
+            t = time.perf_counter()
+            cells, _, _ = O.batch_myers_best_end(seq, pairs["read_pos"], pairs["read_len"],
+                                                 pairs["text_pos"], pairs["text_len"], threads)
+            return cells, time.perf_counter() - t
+        return run_m, sample
     arena, pairs = B.synth_gotoh(seed, sample, config)
     seq = ascii_of_prefix(arena, pairs)
     O.build()
@@ -139,7 +157,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[0, 2])
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2])
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -147,8 +165,8 @@ def main():
     args = ap.parse_args()
     rank, world, local = dist_init(args)
     config = args.config
-    n_pairs = args.pairs or (65536 if config == 0 else 4194304)
-    seed = {0: 1, 2: 3}[config] + 1000 * rank  # weak scaling: each rank its own batch
+    n_pairs = args.pairs or {0: 65536, 1: 1048576, 2: 4194304}[config]
+    seed = {0: 1, 1: 2, 2: 3}[config] + 1000 * rank  # weak scaling: each rank its own batch
     threads = os.cpu_count() or 1
 
     if args.impl == "reference":
@@ -166,7 +184,8 @@ def main():
         line = {"metric": "GCUPS", "value": v, "unit": "GCUPS", "impl": "reference",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "u32" if config == 1 else "int16",
                 "data": "synthetic", "config": {"workload": workload_desc(config, sample),
                                                  "sample_of": n_pairs},
                 "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
@@ -184,30 +203,44 @@ def main():
     import ctypes as C
 
     buf = ExtendBuffer(local)
-    arena, pairs = B.synth_gotoh(seed, n_pairs, config)
-    cells = B.cells_of(pairs)
     stride = 32
-    d_arena = torch.from_numpy(arena).to(f"cuda:{local}")
-    d_pairs = torch.from_numpy(pairs.view(np.uint8)).to(f"cuda:{local}")
-    d_out = torch.empty(n_pairs * B.EXT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{local}")
-    d_cig = torch.empty(n_pairs * stride, dtype=torch.int32, device=f"cuda:{local}")
-    lim = N.BatchLimitsC(int(pairs["read_len"].max()), int(pairs["win_len"].max()),
-                         int(pairs["band_half"].max()))
-    p = ExtendParams()._c()
     L = N.lib()
     stream = torch.cuda.ExternalStream(buf.stream_ptr())
+    p = ExtendParams()._c()
+    if config == 1:
+        arena, pairs = B.synth_myers(seed, n_pairs)
+        cells = int((pairs["read_len"].astype(np.int64) * pairs["text_len"]).sum())
+        res_dtype = B.MYERS_RES_DTYPE
+    else:
+        arena, pairs = B.synth_gotoh(seed, n_pairs, config)
+        cells = B.cells_of(pairs)
+        res_dtype = B.EXT_DTYPE
+    d_arena = torch.from_numpy(arena).to(f"cuda:{local}")
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).to(f"cuda:{local}")
+    d_out = torch.empty(n_pairs * res_dtype.itemsize, dtype=torch.uint8, device=f"cuda:{local}")
+    d_cig = torch.empty(max(1, n_pairs * stride if config != 1 else 1), dtype=torch.int32,
+                        device=f"cuda:{local}")
+    if config == 1:
+        def step():
+            rc = L.esp_batch_myers_device(buf.handle, B.MYERS_BEST_END, d_pairs.data_ptr(),
+                                          n_pairs, 150, d_arena.data_ptr(), arena.nbytes, None,
+                                          0, d_out.data_ptr(), None)
+            buf.check(rc)
+    else:
+        lim = N.BatchLimitsC(int(pairs["read_len"].max()), int(pairs["win_len"].max()),
+                             int(pairs["band_half"].max()))
 
-    def step():
-        rc = L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n_pairs,
-                                       d_arena.data_ptr(), arena.nbytes, None, 0, C.byref(lim),
-                                       C.byref(p), d_out.data_ptr(), d_cig.data_ptr(), stride,
-                                       None)
-        buf.check(rc)
+        def step():
+            rc = L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n_pairs,
+                                           d_arena.data_ptr(), arena.nbytes, None, 0,
+                                           C.byref(lim), C.byref(p), d_out.data_ptr(),
+                                           d_cig.data_ptr(), stride, None)
+            buf.check(rc)
 
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
-    out_host = d_out.cpu().numpy().view(B.EXT_DTYPE)
+    out_host = d_out.cpu().numpy().view(res_dtype)
     bad = int((out_host["status"] != 0).sum())
     if world > 1:
         import torch.distributed as dist
@@ -237,15 +270,21 @@ def main():
 
     # end to end: host arrays (pinned) through the host C-ABI call
     pin_arena = torch.from_numpy(arena).pin_memory().numpy()
-    pin_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory().numpy().view(B.PAIR_DTYPE)
-    out_pin = torch.empty(n_pairs * B.EXT_DTYPE.itemsize, dtype=torch.uint8).pin_memory().numpy()
-    cig_pin = torch.empty(n_pairs * stride, dtype=torch.int32).pin_memory().numpy()
+    pin_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory().numpy()
+    out_pin = torch.empty(n_pairs * res_dtype.itemsize, dtype=torch.uint8).pin_memory().numpy()
+    cig_pin = torch.empty(n_pairs * stride if config != 1 else 1,
+                          dtype=torch.int32).pin_memory().numpy()
 
     def e2e_step():
-        rc = L.esp_batch_extend_host(buf.handle, B.MODE_BAND, pin_pairs.ctypes.data, n_pairs,
-                                     pin_arena.ctypes.data, pin_arena.nbytes, None, 0,
-                                     C.byref(p), out_pin.ctypes.data, cig_pin.ctypes.data,
-                                     stride)
+        if config == 1:
+            rc = L.esp_batch_myers_host(buf.handle, B.MYERS_BEST_END, pin_pairs.ctypes.data,
+                                        n_pairs, pin_arena.ctypes.data, pin_arena.nbytes, None,
+                                        0, out_pin.ctypes.data)
+        else:
+            rc = L.esp_batch_extend_host(buf.handle, B.MODE_BAND, pin_pairs.ctypes.data,
+                                         n_pairs, pin_arena.ctypes.data, pin_arena.nbytes,
+                                         None, 0, C.byref(p), out_pin.ctypes.data,
+                                         cig_pin.ctypes.data, stride)
         buf.check(rc)
     e2e_step()
     t0 = time.perf_counter()
@@ -254,7 +293,7 @@ def main():
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     e2e_val = cells / e2e_s / 1e9
     h2d = pin_arena.nbytes + pin_pairs.nbytes
-    d2h = out_pin.nbytes + cig_pin.nbytes
+    d2h = out_pin.nbytes + (cig_pin.nbytes if config != 1 else 0)
 
     if rank != 0:
         return
@@ -262,7 +301,8 @@ def main():
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     mhz = (clocks or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     peak_ops = sm_count * INT_LANES_PER_SM * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    achieved_ops = cells * OPS_PER_CELL / (ms / 1e3) / 1e12
+    ops_per_cell = MYERS_OPS_PER_CELL if config == 1 else OPS_PER_CELL
+    achieved_ops = cells * ops_per_cell / (ms / 1e3) / 1e12
     cpu = None
     if not args.no_cpu_baseline:
         run, sample = cpu_reference(args, config, n_pairs, seed, threads)
@@ -274,10 +314,11 @@ def main():
     line = {
         "metric": "GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_max,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
-        "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32" if config == 1 else "int16", "data": "synthetic",
         "config": {"workload": workload_desc(config, n_pairs), "pairs": n_pairs,
-                   "cells_per_step": cells, "mode": "run_band",
+                   "cells_per_step": cells,
+                   "mode": "myers_ea::long::infix_best_end" if config == 1 else "run_band",
                    "l2": "inputs larger than L2 (arena %.0f MB + traceback scratch)"
                          % (arena.nbytes / 1e6)},
         "pairs_per_s": n_pairs * world / (ms_max / 1e3),
@@ -287,7 +328,7 @@ def main():
                      "unit": "Tops/s", "frac": achieved_ops / peak_ops, "traffic": None,
                      "peak_source": f"nominal: {sm_count} SMs x {INT_LANES_PER_SM} INT32 lanes x "
                                     f"{peaks.get('sm_max_mhz', 2070.0):.0f} MHz ({src} clock)",
-                     "ops_per_cell": OPS_PER_CELL},
+                     "ops_per_cell": ops_per_cell},
         "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "cpu_baseline": cpu,

@@ -53,6 +53,10 @@ class PairC(C.Structure):
                 ("n_first", C.c_uint32), ("n_read", C.c_uint16), ("n_win", C.c_uint16)]
 
 
+class MyersResultC(C.Structure):
+    _fields_ = [("dist", C.c_int32), ("status", C.c_int32), ("pos", C.c_uint64)]
+
+
 class BatchLimitsC(C.Structure):
     _fields_ = [("max_read_len", C.c_uint32), ("max_win_len", C.c_uint32),
                 ("max_half", C.c_int32)]
@@ -101,6 +105,20 @@ def lib():
     L.esp_batch_extend_device.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
                                           C.c_uint64, C.POINTER(BatchLimitsC),
                                           C.POINTER(ExtendParamsC), vp, vp, C.c_uint32, vp]
+    for name in ("esp_myers_infix", "esp_myers_long_infix"):
+        getattr(L, name).argtypes = [vp, u8p, sz, u8p, sz, C.POINTER(C.c_int32)]
+    for name in ("esp_myers_infix_best_end", "esp_myers_infix_best_start",
+                 "esp_myers_long_infix_best_end", "esp_myers_long_infix_best_start"):
+        getattr(L, name).argtypes = [vp, u8p, sz, u8p, sz, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_uint64)]
+    for name in ("esp_engine_myers_infix", "esp_engine_myers_global"):
+        getattr(L, name).argtypes = [vp, u8p, sz, u8p, sz, C.POINTER(C.c_uint32)]
+    L.esp_batch_myers_device.argtypes = [vp, C.c_int, vp, C.c_uint64, C.c_uint32, vp, C.c_uint64,
+                                         vp, C.c_uint64, vp, vp]
+    L.esp_batch_myers_host.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                       C.c_uint64, vp]
+    L.esp_synth_myers_size.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.esp_synth_myers.argtypes = [C.c_uint64, C.c_uint64, vp, C.c_uint64, vp]
     _lib = L
     return L
 

@@ -24,7 +24,13 @@ EXT_DTYPE = np.dtype([("read_start", "<u4"), ("read_end", "<u4"), ("ref_start", 
                       ("touched", "u1"), ("touch_left", "u1"), ("touch_clamped", "u1"),
                       ("escalated", "u1"), ("status", "<i4")])
 NIV_DTYPE = np.dtype([("start", "<u4"), ("end", "<u4")])
+MYERS_PAIR_DTYPE = np.dtype([("read_pos", "<u8"), ("text_pos", "<u8"), ("read_len", "<u4"),
+                             ("text_len", "<u4"), ("n_first", "<u4"), ("n_read", "<u2"),
+                             ("n_text", "<u2")])
+MYERS_RES_DTYPE = np.dtype([("dist", "<i4"), ("status", "<i4"), ("pos", "<u8")])
 assert PAIR_DTYPE.itemsize == 40 and EXT_DTYPE.itemsize == 32
+assert MYERS_PAIR_DTYPE.itemsize == 32 and MYERS_RES_DTYPE.itemsize == 16
+MYERS_BEST_END, MYERS_BEST_START, MYERS_GLOBAL = 0, 1, 2
 
 MODE_BAND = N.MODE_BAND
 MODE_HINT = N.MODE_HINT
@@ -181,3 +187,47 @@ def extend_batch_host(pairs: np.ndarray, arena: np.ndarray, n_iv: Optional[np.nd
 
 def cigar_of(cig_row: np.ndarray, n_ops: int):
     return [("MIDNS"[int(o) & 15], int(o) >> 4) for o in cig_row[:n_ops]]
+
+
+def synth_myers(seed: int, n_pairs: int):
+    """Seeded Myers workload (config 1): (arena, myers pairs)."""
+    L = N.lib()
+    nb = C.c_uint64()
+    rc = L.esp_synth_myers_size(seed, n_pairs, C.byref(nb))
+    if rc:
+        raise N.EspError(rc, "esp_synth_myers_size")
+    arena = np.zeros(nb.value, np.uint8)
+    pairs = np.zeros(n_pairs, MYERS_PAIR_DTYPE)
+    rc = L.esp_synth_myers(seed, n_pairs, arena.ctypes.data, nb.value, pairs.ctypes.data)
+    if rc:
+        raise N.EspError(rc, "esp_synth_myers")
+    return arena, pairs
+
+
+def pack_ascii_myers(reads, texts):
+    """ASCII read/text pairs -> (arena, myers pairs, n_iv)."""
+    arena, pp, n_iv = pack_ascii_pairs(reads, texts, [0] * len(reads), [0] * len(reads))
+    pairs = np.zeros(len(pp), MYERS_PAIR_DTYPE)
+    pairs["read_pos"] = pp["read_pos"]
+    pairs["text_pos"] = pp["win_pos"]
+    pairs["read_len"] = pp["read_len"]
+    pairs["text_len"] = pp["win_len"]
+    pairs["n_first"] = pp["n_first"]
+    pairs["n_read"] = pp["n_read"]
+    pairs["n_text"] = pp["n_win"]
+    return arena, pairs, n_iv
+
+
+def myers_batch_host(pairs, arena, n_iv=None, mode: int = MYERS_BEST_END,
+                     buf: Optional[ExtendBuffer] = None):
+    buf = buf or _default_buffer()
+    pairs = np.ascontiguousarray(pairs, MYERS_PAIR_DTYPE)
+    arena = np.ascontiguousarray(arena, np.uint8)
+    n_iv = np.zeros(0, NIV_DTYPE) if n_iv is None else np.ascontiguousarray(n_iv, NIV_DTYPE)
+    out = np.zeros(len(pairs), MYERS_RES_DTYPE)
+    rc = N.lib().esp_batch_myers_host(buf.handle, mode, pairs.ctypes.data, len(pairs),
+                                      arena.ctypes.data, len(arena),
+                                      n_iv.ctypes.data if len(n_iv) else None, len(n_iv),
+                                      out.ctypes.data)
+    buf.check(rc)
+    return out

@@ -1,0 +1,131 @@
+// esp_host.h -- host-side state shared by the C-ABI translation units: the
+// handle, error reporting, grow-only buffers and ASCII -> 2-bit encoding.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "esp_internal.h"
+#include "esperanto_gb300.h"
+
+struct esp_handle {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+    int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
+    int variant = -1;   // DP kernel variant; -1 = ESP_GOTOH_VARIANT env or default
+    uint64_t scratch_budget = 8ull << 30;  // bytes of DP scratch one launch may use
+    // grow-only device buffers
+    void *d_in = nullptr;       // per-call staging: pair | n intervals | arena
+    size_t d_in_cap = 0;
+    void *d_res = nullptr;      // per-call results: esp_extension | cigar
+    size_t d_res_cap = 0;
+    uint32_t *d_tb = nullptr;
+    size_t d_tb_cap = 0;        // words
+    uint32_t *d_rb = nullptr;
+    size_t d_rb_cap = 0;
+    uint32_t *d_esc = nullptr;  // escalation list
+    size_t d_esc_cap = 0;       // bytes
+    uint32_t *d_ctr = nullptr;  // [0..1] queues (u64), [4] esc count
+    uint32_t *d_hist = nullptr; // geometry bins
+    size_t d_hist_cap = 0;
+    uint32_t *d_order = nullptr;  // length-binned work list
+    size_t d_order_cap = 0;
+    bool binning = true;
+    // host pinned staging
+    void *h_in = nullptr;
+    size_t h_in_cap = 0;
+    void *h_res = nullptr;
+    size_t h_res_cap = 0;
+    // host batch staging for esp_batch_extend_host
+    void *d_bat = nullptr;
+    size_t d_bat_cap = 0;
+    // Myers per-call / batch staging
+    void *d_my = nullptr;
+    size_t d_my_cap = 0;
+    void *h_my = nullptr;
+    size_t h_my_cap = 0;
+};
+
+inline int fail(esp_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+inline int cuda_fail(esp_handle *h, cudaError_t e, const char *what) {
+    return fail(h, ESP_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, expr)                                        \
+    do {                                                   \
+        cudaError_t _e = (expr);                           \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, #expr); \
+    } while (0)
+
+inline int grow_device(esp_handle *h, void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ESP_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t sz = std::max(need, (size_t)4096);
+    cudaError_t e = cudaMalloc(p, sz);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, ESP_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    *cap = sz;
+    return ESP_OK;
+}
+
+inline int grow_host(esp_handle *h, void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ESP_OK;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t sz = std::max(need * 2, (size_t)65536);
+    cudaError_t e = cudaMallocHost(p, sz);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, ESP_ENOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    *cap = sz;
+    return ESP_OK;
+}
+
+// extend.rs:150-159 base_code folded to the 2-bit arena plus N intervals.
+inline int ascii_code(uint8_t b) {
+    switch (b) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return 4;
+    }
+}
+
+// Append `len` ASCII bases at arena base position `pos` and their N runs.
+inline void encode_seq(const uint8_t *s, size_t len, uint8_t *arena, uint64_t pos,
+                std::vector<esp_n_interval> &iv) {
+    size_t k = 0;
+    while (k < len) {
+        int c = ascii_code(s[k]);
+        if (c == 4) {
+            size_t e = k;
+            while (e < len && ascii_code(s[e]) == 4) e++;
+            iv.push_back({(uint32_t)k, (uint32_t)e});
+            k = e;
+            continue;
+        }
+        uint64_t p = pos + k;
+        arena[p >> 2] |= (uint8_t)(c << (6 - 2 * (p & 3)));
+        k++;
+    }
+}
+

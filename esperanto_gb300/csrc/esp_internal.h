@@ -62,6 +62,20 @@ constexpr int kGotohVariants = 2;
 // Resident blocks per SM of the DP kernel at `block` threads.
 int gotoh_blocks_per_sm(int block, int variant);
 
+// Myers batch job.
+constexpr int MYF_REVERSE = 1;
+constexpr int MYF_GLOBAL = 2;
+struct MyersJob {
+    const esp_myers_pair *pairs;
+    uint64_t n_pairs;
+    const uint8_t *arena;
+    const esp_n_interval *n_iv;
+    int flags;
+    esp_myers_result *out;
+};
+// nw = 32-bit limbs of the longest read (1..8).
+cudaError_t launch_myers(const MyersJob &job, int nw, int num_sms, cudaStream_t st);
+
 // Counting-sort the pairs by geometry (descending cost) into `order`.
 // `hist` needs bin_scratch_bytes() of device memory.  4 launches.
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,

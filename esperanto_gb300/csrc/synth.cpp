@@ -185,4 +185,73 @@ int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
     return ESP_OK;
 }
 
+// Config 1 (Myers): 200-bp uniform text; 90% of queries are 150 bases
+// sampled from the text at a uniform start in [0, 50] with U{0..8} edits
+// (substitution / insertion / deletion, equally likely, at uniform read
+// positions), 10% are unrelated random sequence.
+static void myers_pair_seqs(uint64_t seed, uint64_t i, uint8_t *text, uint8_t *query) {
+    Rng r(pair_seed(seed ^ 0x4D59455253ull, i));
+    for (int k = 0; k < 200; k++) text[k] = r.base();
+    if (r.unit() < 0.1) {
+        for (int k = 0; k < 150; k++) query[k] = r.base();
+        return;
+    }
+    uint32_t start = r.below(51);
+    uint32_t edits = r.below(9);
+    uint8_t kind[150];
+    memset(kind, 0, sizeof(kind));
+    for (uint32_t e = 0; e < edits; e++) kind[r.below(150)] = (uint8_t)(1 + r.below(3));
+    uint32_t s = start, k = 0, p = 0;
+    while (k < 150) {
+        uint8_t kd = p < 150 ? kind[p] : 0;
+        p++;
+        if (kd == 2) {  // insertion
+            query[k++] = r.base();
+            continue;
+        }
+        if (kd == 3) {  // deletion
+            s++;
+            continue;
+        }
+        uint8_t b = s < 200 ? text[s] : r.base();
+        s++;
+        if (kd == 1) b = (uint8_t)((b + 1 + r.below(3)) & 3);
+        query[k++] = b;
+    }
+}
+
+int esp_synth_myers_size(uint64_t seed, uint64_t n_pairs, uint64_t *arena_bytes) {
+    (void)seed;
+    if (!arena_bytes) return ESP_EINVAL;
+    *arena_bytes = (n_pairs * 350 + 3) / 4 + 16;
+    return ESP_OK;
+}
+
+int esp_synth_myers(uint64_t seed, uint64_t n_pairs, uint8_t *arena, uint64_t arena_bytes,
+                    esp_myers_pair *pairs) {
+    if (!arena || !pairs || (n_pairs * 350 + 3) / 4 + 16 > arena_bytes) return ESP_EINVAL;
+    memset(arena, 0, arena_bytes);
+    // 350 bases per pair = 87.5 bytes: pairs of pairs share no byte when the
+    // work is split on even pair indices (700 bases = 175 whole bytes).
+    uint64_t groups = (n_pairs + 1) / 2;
+    parallel_for(groups, [&](uint64_t g) {
+        uint8_t text[200], query[150];
+        for (uint64_t i = 2 * g; i < 2 * g + 2 && i < n_pairs; i++) {
+            myers_pair_seqs(seed, i, text, query);
+            uint64_t p = i * 350;
+            for (int k = 0; k < 150; k++) put2(arena, p + k, query[k]);
+            for (int k = 0; k < 200; k++) put2(arena, p + 150 + k, text[k]);
+            esp_myers_pair &P = pairs[i];
+            P.read_pos = p;
+            P.text_pos = p + 150;
+            P.read_len = 150;
+            P.text_len = 200;
+            P.n_first = 0;
+            P.n_read = 0;
+            P.n_text = 0;
+        }
+    });
+    return ESP_OK;
+}
+
 }  // extern "C"

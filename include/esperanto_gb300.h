@@ -167,6 +167,73 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
                           const esp_extend_params *params, esp_extension *out,
                           uint32_t *cigar, uint32_t cigar_stride);
 
+/* ---- EA-Myers filters: crates/map/src/myers_ea.rs, crates/engine/src/myers.rs ----
+ *
+ * Editing-aware equality: read A matches reference {A}, C matches {C,T},
+ * G matches {G,A}, T matches {T}; anything else matches nothing; case
+ * folds.  Per-call entry points take ASCII like the reference. */
+
+/* myers_ea::infix (myers_ea.rs:118-135): min distance of the whole read
+ * against any substring of `text`.  m = 0 -> 0; m > 256 -> m; the
+ * single-block entry points refuse 128 < m <= 256 (ESP_EINVAL), which the
+ * reference's callers route to long:: (align.rs:878-882). */
+int esp_myers_infix(esp_handle *h, const uint8_t *read, size_t m, const uint8_t *text,
+                    size_t n, int32_t *dist);
+/* myers_ea::infix_best_end (myers_ea.rs:138-155): also the earliest
+ * exclusive end of a best occurrence (0 when nothing beats m). */
+int esp_myers_infix_best_end(esp_handle *h, const uint8_t *read, size_t m, const uint8_t *text,
+                             size_t n, int32_t *dist, uint64_t *end);
+/* myers_ea::infix_best_start(_into) (myers_ea.rs:158-185): best_end of the
+ * reversed pair, start = n - reversed end. */
+int esp_myers_infix_best_start(esp_handle *h, const uint8_t *read, size_t m,
+                               const uint8_t *text, size_t n, int32_t *dist, uint64_t *start);
+/* myers_ea::long::{infix, infix_best_end, infix_best_start(_into)}
+ * (myers_ea.rs:249-310): the same for m <= 256. */
+int esp_myers_long_infix(esp_handle *h, const uint8_t *read, size_t m, const uint8_t *text,
+                         size_t n, int32_t *dist);
+int esp_myers_long_infix_best_end(esp_handle *h, const uint8_t *read, size_t m,
+                                  const uint8_t *text, size_t n, int32_t *dist, uint64_t *end);
+int esp_myers_long_infix_best_start(esp_handle *h, const uint8_t *read, size_t m,
+                                    const uint8_t *text, size_t n, int32_t *dist,
+                                    uint64_t *start);
+/* esperanto_engine::myers::{infix, long::infix} (engine/src/myers.rs:32-56)
+ * and {global, long::global} (:42-62); 1 <= m <= 256 (the reference asserts,
+ * here ESP_EINVAL). */
+int esp_engine_myers_infix(esp_handle *h, const uint8_t *read, size_t m, const uint8_t *text,
+                           size_t n, uint32_t *dist);
+int esp_engine_myers_global(esp_handle *h, const uint8_t *read, size_t m, const uint8_t *text,
+                            size_t n, uint32_t *dist);
+
+/* Batch Myers (new): pairs over a 2-bit arena as for the DP batch. */
+typedef struct {
+    uint64_t read_pos;
+    uint64_t text_pos;
+    uint32_t read_len;  /* 1..256 */
+    uint32_t text_len;
+    uint32_t n_first;   /* N intervals: read's, then text's */
+    uint16_t n_read;
+    uint16_t n_text;
+} esp_myers_pair;
+
+typedef struct {
+    int32_t dist;
+    int32_t status;
+    uint64_t pos;       /* best end (exclusive) or best start (inclusive) */
+} esp_myers_result;
+
+#define ESP_MYERS_BEST_END 0   /* myers_ea::infix_best_end / long:: */
+#define ESP_MYERS_BEST_START 1 /* myers_ea::infix_best_start / long:: */
+#define ESP_MYERS_GLOBAL 2     /* engine::myers::global (pos = 0) */
+
+int esp_batch_myers_device(esp_handle *h, int mode, const esp_myers_pair *pairs,
+                           uint64_t n_pairs, uint32_t max_read_len, const uint8_t *arena,
+                           uint64_t arena_bytes, const esp_n_interval *n_iv,
+                           uint64_t n_iv_count, esp_myers_result *out, void *stream);
+int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
+                         uint64_t n_pairs, const uint8_t *arena, uint64_t arena_bytes,
+                         const esp_n_interval *n_iv, uint64_t n_iv_count,
+                         esp_myers_result *out);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----
  *
  * esp_batch_run_band_noalloc: the same banded/full-matrix DP with traceback
@@ -210,6 +277,12 @@ int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int config, uint64_t *
 /* Fill the workload into caller memory (host). */
 int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
                     uint64_t arena_bytes, esp_pair *pairs);
+
+/* Myers workload: 150-bp queries sampled from 200-bp uniform texts with
+ * U{0..8} edits, 10% unrelated random queries (config 1). */
+int esp_synth_myers_size(uint64_t seed, uint64_t n_pairs, uint64_t *arena_bytes);
+int esp_synth_myers(uint64_t seed, uint64_t n_pairs, uint8_t *arena, uint64_t arena_bytes,
+                    esp_myers_pair *pairs);
 
 /* Number of device kernel launches the last batch call enqueued. */
 uint64_t esp_last_launch_count(const esp_handle *h);
