@@ -57,6 +57,28 @@ class MyersResultC(C.Structure):
     _fields_ = [("dist", C.c_int32), ("status", C.c_int32), ("pos", C.c_uint64)]
 
 
+class ContigC(C.Structure):
+    _fields_ = [("base", C.c_uint64), ("len", C.c_uint32), ("n_first", C.c_uint32),
+                ("n_count", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class JunctionC(C.Structure):
+    _fields_ = [("contig", C.c_uint32), ("start", C.c_uint32), ("end", C.c_uint32),
+                ("minus_strand", C.c_int32)]
+
+
+class SpliceParamsC(C.Structure):
+    _fields_ = [("min_intron", C.c_uint32), ("max_intron", C.c_uint32),
+                ("gt_ag_bonus", C.c_int32), ("gc_ag_bonus", C.c_int32),
+                ("at_ac_bonus", C.c_int32), ("noncanonical_penalty", C.c_int32),
+                ("known_bonus", C.c_int32), ("refine_radius", C.c_uint32)]
+
+
+class RetryOutcomeC(C.Structure):
+    _fields_ = [("found", C.c_int32), ("dro", C.c_uint32), ("left_win_lo", C.c_uint32),
+                ("total", C.c_int32), ("left", ExtensionC), ("right", ExtensionC)]
+
+
 class BatchLimitsC(C.Structure):
     _fields_ = [("max_read_len", C.c_uint32), ("max_win_len", C.c_uint32),
                 ("max_half", C.c_int32)]
@@ -119,6 +141,21 @@ def lib():
                                        C.c_uint64, vp]
     L.esp_synth_myers_size.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]
     L.esp_synth_myers.argtypes = [C.c_uint64, C.c_uint64, vp, C.c_uint64, vp]
+    L.esp_genome_create.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint32, vp, C.c_uint64,
+                                    C.POINTER(vp)]
+    L.esp_genome_destroy.argtypes = [vp]
+    L.esp_retry_tail_start.argtypes = [vp, vp, u8p, sz, C.c_uint32, C.POINTER(JunctionC), C.c_int,
+                                       C.c_uint32, C.POINTER(SpliceParamsC),
+                                       C.POINTER(ExtendParamsC), C.POINTER(RetryOutcomeC), vp, vp,
+                                       C.c_uint32]
+    L.esp_batch_splice_host.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64,
+                                        vp, C.c_uint64, C.POINTER(SpliceParamsC),
+                                        C.POINTER(ExtendParamsC), vp, vp, C.c_uint32]
+    L.esp_last_cells.argtypes = [vp]
+    L.esp_last_cells.restype = C.c_uint64
+    L.esp_synth_splice_size.argtypes = [C.c_uint64, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3
+    L.esp_synth_splice.argtypes = [C.c_uint64, C.c_uint64, vp, C.c_uint64, vp, vp, C.c_uint64,
+                                   vp, vp, C.c_uint64]
     _lib = L
     return L
 

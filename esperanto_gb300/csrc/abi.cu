@@ -14,25 +14,14 @@
 
 namespace {
 
-struct Limits {
-    uint64_t tb_words = 1, rb_words = 1;
-    uint32_t max_m = 0;
-};
-
-void add_limits(Limits &L, uint32_t m, uint32_t n, int32_t half) {
-    uint64_t tb, rb;
-    esp::gotoh_scratch_words(m, n, half, tb, rb);
-    L.tb_words = std::max(L.tb_words, tb);
-    L.rb_words = std::max(L.rb_words, rb);
-    L.max_m = std::max(L.max_m, m);
-}
+}  // namespace
 
 // Enqueue the DP launches of one batch whose inputs are on the device.
 int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_pairs,
                   const uint8_t *d_arena, uint64_t arena_bytes, const esp_n_interval *d_iv,
                   uint64_t n_iv, const esp::GotohConst &K, const Limits &L1, const Limits &L2,
                   esp_extension *d_out, uint32_t *d_cigar, uint32_t cigar_stride,
-                  cudaStream_t st) {
+                  cudaStream_t st, const uint8_t *d_win_arena, uint64_t win_arena_bytes) {
     h->launches = 0;
     if (n_pairs == 0) return ESP_OK;
     if (n_pairs > 0xffffffffull - 64) return fail(h, ESP_EINVAL, "batch too large");
@@ -79,6 +68,8 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     job.n_pairs = n_pairs;
     job.arena = d_arena;
     job.arena_bases = arena_bytes * 4;
+    job.win_arena = d_win_arena;
+    job.win_arena_bases = win_arena_bytes * 4;
     job.n_iv = d_iv;
     job.n_iv_count = n_iv;
     job.out = d_out;
@@ -108,7 +99,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     return ESP_OK;
 }
 
-}  // namespace
+
 
 extern "C" {
 
@@ -142,6 +133,8 @@ int esp_destroy(esp_handle *h) {
     cudaFree(h->d_ctr);
     cudaFree(h->d_bat);
     cudaFree(h->d_my);
+    cudaFree(h->d_spl);
+    cudaFree(h->d_spl_io);
     if (h->h_my) cudaFreeHost(h->h_my);
     cudaFree(h->d_hist);
     cudaFree(h->d_order);

@@ -92,6 +92,51 @@ __global__ void bin_scatter(const esp_pair *__restrict__ pairs, uint64_t n, int 
     }
 }
 
+// Window width summed over rows 1..m (extend.rs:653-696).
+__device__ uint64_t band_cells(uint32_t m, uint32_t n, int64_t off, int64_t half) {
+    uint64_t cells = 0;
+    for (uint32_t i = 1; i <= m; i++) {
+        int64_t c = off + i;
+        c = c < 1 ? 1 : (c > n ? n : c);
+        int64_t lo = c - half > 1 ? c - half : 1;
+        int64_t hi = c + half < (int64_t)n ? c + half : (int64_t)n;
+        if (hi >= lo) cells += (uint64_t)(hi - lo + 1);
+    }
+    return cells;
+}
+
+__global__ void count_cells(const esp_pair *__restrict__ pairs,
+                            const esp_extension *__restrict__ out, uint64_t n, int mode,
+                            unsigned long long *cells) {
+    uint64_t acc = 0;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const esp_pair P = pairs[k];
+        uint32_t m = P.read_len, w = P.win_len;
+        if (m == 0 || w == 0) continue;
+        if (mode == 0) {
+            acc += P.band_half < 0 ? (uint64_t)m * w : band_cells(m, w, P.band_offset, P.band_half);
+        } else if (w <= 30) {
+            acc += (uint64_t)m * w;
+        } else {
+            acc += band_cells(m, w, P.band_offset, 30);
+            if (out[k].escalated) acc += (uint64_t)m * w;
+        }
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(cells, (unsigned long long)acc);
+}
+
+cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, uint64_t n,
+                               int mode, unsigned long long *cells, int num_sms,
+                               cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    uint64_t need = (n + 255) / 256;
+    int grid = (int)(need < (uint64_t)num_sms * 8 ? need : (uint64_t)num_sms * 8);
+    count_cells<<<grid, 256, 0, st>>>(pairs, out, n, mode, cells);
+    return cudaGetLastError();
+}
+
 size_t bin_scratch_bytes() { return (size_t)NBINS * sizeof(uint32_t); }
 
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,

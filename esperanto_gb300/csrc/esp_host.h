@@ -47,6 +47,12 @@ struct esp_handle {
     // host batch staging for esp_batch_extend_host
     void *d_bat = nullptr;
     size_t d_bat_cap = 0;
+    uint64_t last_cells = 0;    // DP cells of the last splice batch
+    // splice batch scratch
+    void *d_spl = nullptr;
+    size_t d_spl_cap = 0;
+    void *d_spl_io = nullptr;   // host-API staging of reads / candidates / results
+    size_t d_spl_io_cap = 0;
     // Myers per-call / batch staging
     void *d_my = nullptr;
     size_t d_my_cap = 0;
@@ -129,3 +135,38 @@ inline void encode_seq(const uint8_t *s, size_t len, uint8_t *arena, uint64_t po
     }
 }
 
+
+struct Limits {
+    uint64_t tb_words = 1, rb_words = 1;
+    uint32_t max_m = 0;
+};
+
+inline void add_limits(Limits &L, uint32_t m, uint32_t n, int32_t half) {
+    uint64_t tb, rb;
+    esp::gotoh_scratch_words(m, n, half, tb, rb);
+    L.tb_words = std::max(L.tb_words, tb);
+    L.rb_words = std::max(L.rb_words, rb);
+    L.max_m = std::max(L.max_m, m);
+}
+
+
+// Enqueue the DP launches of one batch whose inputs are on the device
+// (abi.cu).  Windows come from d_win_arena when it is not null.
+int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_pairs,
+                  const uint8_t *d_arena, uint64_t arena_bytes, const esp_n_interval *d_iv,
+                  uint64_t n_iv, const esp::GotohConst &K, const Limits &L1, const Limits &L2,
+                  esp_extension *d_out, uint32_t *d_cigar, uint32_t cigar_stride,
+                  cudaStream_t st, const uint8_t *d_win_arena = nullptr,
+                  uint64_t win_arena_bytes = 0);
+
+// Resident genome (esp_genome_create): device arena + contig table + N table,
+// with host copies of the small tables for host-side validation.
+struct esp_genome {
+    int device = 0;
+    uint8_t *d_arena = nullptr;
+    uint64_t arena_bytes = 0;
+    esp_contig *d_contigs = nullptr;
+    std::vector<esp_contig> contigs;
+    esp_n_interval *d_iv = nullptr;
+    uint64_t n_iv = 0;
+};

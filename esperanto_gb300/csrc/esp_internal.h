@@ -35,8 +35,10 @@ struct GotohJob {
     uint64_t n_pairs;
     const uint32_t *list;       // optional: indices into pairs (device); null = 0..n-1
     const uint32_t *list_count; // optional device counter (when list is a queue)
-    const uint8_t *arena;
-    uint64_t arena_bases;       // bases addressable in the arena (excluding padding)
+    const uint8_t *arena;       // arena of the reads
+    uint64_t arena_bases;       // bases addressable in it (excluding padding)
+    const uint8_t *win_arena;   // arena of the windows (null = same as reads)
+    uint64_t win_arena_bases;
     const esp_n_interval *n_iv;
     uint64_t n_iv_count;
     int mode;                   // 0 band/full per pair, 1 hint attempt 1, 2 hint attempt 2
@@ -75,6 +77,54 @@ struct MyersJob {
 };
 // nw = 32-bit limbs of the longest read (1..8).
 cudaError_t launch_myers(const MyersJob &job, int nw, int num_sms, cudaStream_t st);
+
+// Splice-rescue batch (splice.cu).
+constexpr int SPL_SLOTS = 22;  // 11 breakpoints x (left, right) per candidate
+constexpr int SPL_IVCAP = 6;   // N intervals one DP slot can carry (read + window)
+struct SpliceItem {
+    int32_t valid;   // candidate survives channel A's filters
+    int32_t signal;  // ESP_SIG_*
+};
+struct SpliceItemOut {  // retry_tail_start outcome of one candidate
+    int32_t found;
+    uint32_t dro;
+    uint32_t left_win_lo;
+    int32_t total;
+    uint64_t slot;        // DP slot of the left segment (right = slot + 1)
+};
+struct SpliceJob {
+    int retry_only;       // per-call retry_tail_start: no channel-A filters,
+    int forced_signal;    // the caller's signal is used
+    SpliceItemOut *item_out;  // optional per-candidate outcome
+    const esp_splice_read *reads;
+    uint64_t n_reads;
+    const uint8_t *read_arena;
+    const esp_n_interval *read_iv;
+    const uint8_t *g_arena;
+    const esp_contig *contigs;
+    uint32_t n_contigs;
+    const esp_n_interval *g_iv;
+    const esp_splice_cand *cands;
+    esp_splice_params sp;
+    SpliceItem *items;           // one per candidate
+    int32_t *read_status;        // one per read
+    esp_pair *dp_pairs;          // SPL_SLOTS per candidate
+    esp_n_interval *dp_iv;       // SPL_IVCAP per slot, or null when no N anywhere
+    const esp_extension *dp_out;
+    const uint32_t *dp_cig;
+    uint32_t dp_stride;
+    esp_splice_result *out;
+    uint32_t *cigar;
+    uint32_t cigar_stride;
+};
+cudaError_t launch_splice_build(const SpliceJob &J, int num_sms, cudaStream_t st);
+cudaError_t launch_splice_select(const SpliceJob &J, int num_sms, cudaStream_t st);
+
+// DP cells of a finished batch (sum over rows of the window width of every
+// attempt that ran), accumulated into *cells (u64, zeroed by the caller).
+cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, uint64_t n,
+                               int mode, unsigned long long *cells, int num_sms,
+                               cudaStream_t st);
 
 // Counting-sort the pairs by geometry (descending cost) into `order`.
 // `hist` needs bin_scratch_bytes() of device memory.  4 launches.

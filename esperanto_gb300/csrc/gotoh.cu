@@ -635,8 +635,10 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
         job.out[pi] = o;
         return;
     }
+    const uint8_t *warena = job.win_arena ? job.win_arena : job.arena;
+    const uint64_t wbases = job.win_arena ? job.win_arena_bases : job.arena_bases;
     if ((uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
-        P.read_pos + (uint64_t)m > job.arena_bases || P.win_pos + (uint64_t)n > job.arena_bases ||
+        P.read_pos + (uint64_t)m > job.arena_bases || P.win_pos + (uint64_t)n > wbases ||
         m > 32767 || n > 32767) {
         o.status = ESP_EINVAL;  // pair outside the arena / N table: refuse
         job.out[pi] = o;
@@ -644,7 +646,7 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     }
     const esp_n_interval *iv = job.n_iv + P.n_first;
     Seq read{job.arena, P.read_pos, iv, P.n_read};
-    Seq win{job.arena, P.win_pos, iv + P.n_read, P.n_win};
+    Seq win{warena, P.win_pos, iv + P.n_read, P.n_win};
     FillResult F = win.cnt ? dp_fill<true>(K, s_lut, m, n, g, read, win, tb, sw, rb)
                            : dp_fill<false>(K, s_lut, m, n, g, read, win, tb, sw, rb);
     dp_finish(K, lut, g, tb, sw, m, n, read, win, F, o, cig, job.cigar_stride);

@@ -254,4 +254,137 @@ int esp_synth_myers(uint64_t seed, uint64_t n_pairs, uint8_t *arena, uint64_t ar
     return ESP_OK;
 }
 
+// Config 3 (splice): one contig per read.  Draw order per read (shared by
+// the sizing and filling passes): intron length, breakpoint, tail jitter,
+// decoy donors, decoy acceptors, supports, then sequence.
+struct SpliceShape {
+    uint32_t intron, b, ts;
+    uint32_t n_dd, n_da;
+    int8_t dd[41], da[41];   // decoy offsets from the true donor / acceptor
+    uint32_t sup_true;
+    uint8_t sup_d[41], sup_a[41];
+};
+
+static SpliceShape splice_shape(Rng &r) {
+    SpliceShape s;
+    double lu = std::log(60.0) + r.unit() * (std::log(50000.0) - std::log(60.0));
+    s.intron = (uint32_t)std::exp(lu);
+    if (s.intron < 60) s.intron = 60;
+    s.b = 20 + r.below(111);
+    int ts = (int)s.b + (int)r.below(7) - 3;
+    s.ts = (uint32_t)(ts < 1 ? 1 : (ts > 149 ? 149 : ts));
+    s.n_dd = s.n_da = 0;
+    for (int k = -20; k <= 20; k++)
+        if (k != 0 && r.below(16) == 0) s.dd[s.n_dd++] = (int8_t)k;
+    for (int k = -20; k <= 20; k++)
+        if (k != 0 && r.below(16) == 0) s.da[s.n_da++] = (int8_t)k;
+    s.sup_true = 3 + r.below(8);
+    for (uint32_t k = 0; k < s.n_dd; k++) s.sup_d[k] = (uint8_t)(1 + r.below(3));
+    for (uint32_t k = 0; k < s.n_da; k++) s.sup_a[k] = (uint8_t)(1 + r.below(3));
+    return s;
+}
+
+int esp_synth_splice_size(uint64_t seed, uint64_t n_reads, uint64_t *genome_bytes,
+                          uint64_t *read_bytes, uint64_t *n_cands) {
+    if (!genome_bytes || !read_bytes || !n_cands) return ESP_EINVAL;
+    std::vector<uint64_t> g(n_reads), c(n_reads);
+    parallel_for(n_reads, [&](uint64_t i) {
+        Rng r(pair_seed(seed ^ 0x53504C43ull, i));
+        SpliceShape s = splice_shape(r);
+        g[i] = 600 + s.intron;
+        c[i] = 1 + s.n_dd + s.n_da;
+    });
+    uint64_t gb = 0, cc = 0;
+    for (uint64_t i = 0; i < n_reads; i++) {
+        gb += (g[i] + 3) / 4 * 4;  // contigs start on whole bytes
+        cc += c[i];
+    }
+    *genome_bytes = gb / 4 + 16;
+    *read_bytes = (n_reads * 150 + 3) / 4 + 16;
+    *n_cands = cc;
+    return ESP_OK;
+}
+
+int esp_synth_splice(uint64_t seed, uint64_t n_reads, uint8_t *genome_arena,
+                     uint64_t genome_bytes, esp_contig *contigs, uint8_t *read_arena,
+                     uint64_t read_bytes, esp_splice_read *reads, esp_splice_cand *cands,
+                     uint64_t n_cands) {
+    if (!genome_arena || !contigs || !read_arena || !reads || !cands) return ESP_EINVAL;
+    std::vector<SpliceShape> shp(n_reads);
+    parallel_for(n_reads, [&](uint64_t i) {
+        Rng r(pair_seed(seed ^ 0x53504C43ull, i));
+        shp[i] = splice_shape(r);
+    });
+    std::vector<uint64_t> gpos(n_reads + 1, 0), cpos(n_reads + 1, 0);
+    for (uint64_t i = 0; i < n_reads; i++) {
+        gpos[i + 1] = gpos[i] + (600 + shp[i].intron + 3) / 4 * 4;
+        cpos[i + 1] = cpos[i] + 1 + shp[i].n_dd + shp[i].n_da;
+    }
+    if (gpos[n_reads] / 4 + 16 > genome_bytes || cpos[n_reads] > n_cands ||
+        (n_reads * 150 + 3) / 4 + 16 > read_bytes)
+        return ESP_EINVAL;
+    memset(genome_arena, 0, genome_bytes);
+    memset(read_arena, 0, read_bytes);
+    // reads pack 150 bases = 37.5 bytes: split the work on even read indices
+    uint64_t groups = (n_reads + 1) / 2;
+    parallel_for(groups, [&](uint64_t grp) {
+        std::vector<uint8_t> ctg, src(200), rd(150);
+        for (uint64_t i = 2 * grp; i < 2 * grp + 2 && i < n_reads; i++) {
+            Rng r(pair_seed(seed ^ 0x53504C43ull, i));
+            SpliceShape s = splice_shape(r);
+            uint32_t len = 600 + s.intron, d0 = 300, a0 = 300 + s.intron;
+            ctg.resize(len);
+            for (uint32_t k = 0; k < len; k++) ctg[k] = r.base();
+            for (uint32_t k = 0; k < s.n_dd; k++) {  // decoy GT donors
+                uint32_t p = d0 + s.dd[k];
+                ctg[p] = 2;
+                ctg[p + 1] = 3;
+            }
+            for (uint32_t k = 0; k < s.n_da; k++) {  // decoy AG acceptors (end at p)
+                uint32_t p = a0 + s.da[k];
+                ctg[p - 2] = 0;
+                ctg[p - 1] = 2;
+            }
+            ctg[d0] = 2;  // true GT..AG
+            ctg[d0 + 1] = 3;
+            ctg[a0 - 2] = 0;
+            ctg[a0 - 1] = 2;
+            for (uint32_t k = 0; k < len; k++) put2(genome_arena, gpos[i] + k, ctg[k]);
+            // spliced source: exon1[300-b, 300) + exon2[0, ...)
+            for (uint32_t k = 0; k < 200; k++)
+                src[k] = k < s.b ? ctg[d0 - s.b + k] : (a0 + (k - s.b) < len ? ctg[a0 + (k - s.b)] : 0);
+            derive_read(r, src.data(), 200, 0, 150, rd.data());
+            for (uint32_t k = 0; k < 150; k++) put2(read_arena, i * 150 + k, rd[k]);
+            esp_contig &C = contigs[i];
+            C.base = gpos[i];
+            C.len = len;
+            C.n_first = 0;
+            C.n_count = 0;
+            C.pad = 0;
+            esp_splice_read &R = reads[i];
+            R.read_pos = i * 150;
+            R.read_len = 150;
+            R.tail_start = s.ts;
+            R.contig = (uint32_t)i;
+            R.minus = 0;
+            R.cand_first = (uint32_t)cpos[i];
+            R.cand_count = (uint32_t)(cpos[i + 1] - cpos[i]);
+            R.n_first = 0;
+            R.n_read = 0;
+            // library order: sorted by (start, end)
+            std::vector<esp_splice_cand> cs;
+            cs.push_back({{(uint32_t)i, d0, a0, 0}, s.sup_true});
+            for (uint32_t k = 0; k < s.n_dd; k++)
+                cs.push_back({{(uint32_t)i, (uint32_t)(d0 + s.dd[k]), a0, 0}, s.sup_d[k]});
+            for (uint32_t k = 0; k < s.n_da; k++)
+                cs.push_back({{(uint32_t)i, d0, (uint32_t)(a0 + s.da[k]), 0}, s.sup_a[k]});
+            std::sort(cs.begin(), cs.end(), [](const esp_splice_cand &x, const esp_splice_cand &y) {
+                return x.j.start != y.j.start ? x.j.start < y.j.start : x.j.end < y.j.end;
+            });
+            for (size_t k = 0; k < cs.size(); k++) cands[cpos[i] + k] = cs[k];
+        }
+    });
+    return ESP_OK;
+}
+
 }  // extern "C"

@@ -1,0 +1,209 @@
+"""Host mirror of the splice-rescue flank DP of crates/map/src/split.rs over
+the GB300 kernels, plus the resident genome it reads windows from.
+
+* ``Genome``            -- the reference's ``Reference`` (fasta.rs:62-75):
+                           2-bit contigs + N intervals, resident in HBM.
+* ``retry_tail_start``  -- split.rs:150-223 (same arguments and result).
+* ``channel_a_batch``   -- channel A (split.rs:468-570) over many reads, each
+                           with its library candidates, + build_rescue_ext.
+Every DP runs on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _native as N
+from . import batch as B
+from .extend import (ExtendBuffer, ExtendParams, Extension, _b, _default_buffer,
+                     decode_cigar)
+
+SIG_GTAG, SIG_GCAG, SIG_ATAC, SIG_NONCANONICAL = 0, 1, 2, 3
+
+CONTIG_DTYPE = np.dtype([("base", "<u8"), ("len", "<u4"), ("n_first", "<u4"),
+                         ("n_count", "<u4"), ("pad", "<u4")])
+SPLICE_READ_DTYPE = np.dtype([("read_pos", "<u8"), ("read_len", "<u4"), ("tail_start", "<u4"),
+                              ("contig", "<u4"), ("minus", "<i4"), ("cand_first", "<u4"),
+                              ("cand_count", "<u4"), ("n_first", "<u4"), ("n_read", "<u4")])
+SPLICE_CAND_DTYPE = np.dtype([("contig", "<u4"), ("start", "<u4"), ("end", "<u4"),
+                              ("minus_strand", "<i4"), ("support", "<u4")])
+SPLICE_RES_DTYPE = np.dtype([("found", "<i4"), ("cand", "<i4"), ("dro", "<u4"), ("pos", "<u4"),
+                             ("score", "<i4"), ("signal", "<i4"), ("n_ops", "<u4"),
+                             ("status", "<i4")])
+
+
+@dataclass
+class SpliceParams:
+    """splice.rs:21-53 SpliceParams::default()."""
+    min_intron: int = 20
+    max_intron: int = 1_000_000
+    gt_ag_bonus: int = 4
+    gc_ag_bonus: int = 2
+    at_ac_bonus: int = 1
+    noncanonical_penalty: int = 8
+    known_bonus: int = 6
+    refine_radius: int = 12
+
+    def _c(self):
+        return N.SpliceParamsC(self.min_intron, self.max_intron, self.gt_ag_bonus,
+                               self.gc_ag_bonus, self.at_ac_bonus, self.noncanonical_penalty,
+                               self.known_bonus, self.refine_radius)
+
+
+@dataclass
+class Junction:
+    """gtf.rs:23-32."""
+    contig: int
+    start: int
+    end: int
+    minus_strand: bool = False
+
+
+@dataclass
+class RetryOutcome:
+    """split.rs:120-132."""
+    dro: int
+    left_win_lo: int
+    left: Extension
+    right: Extension
+    total: int
+
+
+class Genome:
+    """A resident 2-bit genome: contigs packed MSB-first with their N runs."""
+
+    def __init__(self, arena: np.ndarray, contigs: np.ndarray, n_iv: Optional[np.ndarray] = None,
+                 buf: Optional[ExtendBuffer] = None):
+        self.buf = buf or _default_buffer()
+        self.arena = np.ascontiguousarray(arena, np.uint8)
+        self.contigs = np.ascontiguousarray(contigs, CONTIG_DTYPE)
+        self.n_iv = (np.zeros(0, B.NIV_DTYPE) if n_iv is None
+                     else np.ascontiguousarray(n_iv, B.NIV_DTYPE))
+        g = C.c_void_p()
+        rc = N.lib().esp_genome_create(self.buf.handle, self.arena.ctypes.data, len(self.arena),
+                                       self.contigs.ctypes.data, len(self.contigs),
+                                       self.n_iv.ctypes.data if len(self.n_iv) else None,
+                                       len(self.n_iv), C.byref(g))
+        self.buf.check(rc)
+        self._g = g
+
+    @classmethod
+    def from_sequences(cls, seqs: Sequence, buf: Optional[ExtendBuffer] = None) -> "Genome":
+        """Contigs from ASCII sequences (non-ACGT -> N intervals)."""
+        codes, contigs, ivs = [], np.zeros(len(seqs), CONTIG_DTYPE), []
+        base = 0
+        for c, s in enumerate(seqs):
+            s = _b(s)
+            arr = B._CODE[np.frombuffer(s, np.uint8)] if len(s) else np.zeros(0, np.uint8)
+            isn = arr == 4
+            runs = []
+            k = 0
+            while k < len(arr):
+                if isn[k]:
+                    e = k
+                    while e < len(arr) and isn[e]:
+                        e += 1
+                    runs.append((k, e))
+                    k = e
+                else:
+                    k += 1
+            contigs[c] = (base, len(s), len(ivs), len(runs), 0)
+            ivs.extend(runs)
+            pad = (-len(arr)) % 4
+            codes.append(np.concatenate([arr, np.zeros(pad, np.uint8)]))
+            base += len(arr) + pad
+        allc = np.concatenate(codes) if codes else np.zeros(0, np.uint8)
+        n_iv = np.array(ivs, dtype=np.uint32).reshape(-1, 2)
+        iv = np.zeros(len(n_iv), B.NIV_DTYPE)
+        if len(n_iv):
+            iv["start"], iv["end"] = n_iv[:, 0], n_iv[:, 1]
+        return cls(B.pack_codes(allc), contigs, iv, buf)
+
+    @property
+    def handle(self):
+        return self._g
+
+    def close(self):
+        if getattr(self, "_g", None):
+            N.lib().esp_genome_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def retry_tail_start(genome: Genome, read, tail_start: int, j: Junction, signal: int,
+                     support: int, params: SpliceParams = SpliceParams(),
+                     extend_params: ExtendParams = ExtendParams(),
+                     buf: Optional[ExtendBuffer] = None) -> Optional[RetryOutcome]:
+    """split.rs:150-223 on the GPU."""
+    buf = buf or genome.buf
+    read = _b(read)
+    cap = 2 * len(read) + 16
+    lc, rc_ = (C.c_uint32 * cap)(), (C.c_uint32 * cap)()
+    out = N.RetryOutcomeC()
+    jc = N.JunctionC(j.contig, j.start, j.end, int(j.minus_strand))
+    sp, p = params._c(), extend_params._c()
+    rc = N.lib().esp_retry_tail_start(buf.handle, genome.handle, read, len(read), tail_start,
+                                      C.byref(jc), signal, support, C.byref(sp), C.byref(p),
+                                      C.byref(out), lc, rc_, cap)
+    buf.check(rc)
+    if not out.found:
+        return None
+    le = Extension(out.left.read_start, out.left.read_end, out.left.ref_start,
+                   decode_cigar(lc[:out.left.n_ops]), out.left.score)
+    re = Extension(out.right.read_start, out.right.read_end, out.right.ref_start,
+                   decode_cigar(rc_[:out.right.n_ops]), out.right.score)
+    return RetryOutcome(out.dro, out.left_win_lo, le, re, out.total)
+
+
+def channel_a_batch(genome: Genome, reads: np.ndarray, read_arena: np.ndarray,
+                    cands: np.ndarray, read_n_iv: Optional[np.ndarray] = None,
+                    params: SpliceParams = SpliceParams(),
+                    extend_params: ExtendParams = ExtendParams(), cigar_stride: int = 64,
+                    buf: Optional[ExtendBuffer] = None):
+    """Channel A over a batch: returns (results, cigars, dp_cells)."""
+    buf = buf or genome.buf
+    reads = np.ascontiguousarray(reads, SPLICE_READ_DTYPE)
+    cands = np.ascontiguousarray(cands, SPLICE_CAND_DTYPE)
+    read_arena = np.ascontiguousarray(read_arena, np.uint8)
+    iv = (np.zeros(0, B.NIV_DTYPE) if read_n_iv is None
+          else np.ascontiguousarray(read_n_iv, B.NIV_DTYPE))
+    out = np.zeros(len(reads), SPLICE_RES_DTYPE)
+    cig = np.zeros(max(1, len(reads) * cigar_stride), np.uint32)
+    sp, p = params._c(), extend_params._c()
+    rc = N.lib().esp_batch_splice_host(buf.handle, genome.handle, reads.ctypes.data, len(reads),
+                                       read_arena.ctypes.data, len(read_arena),
+                                       iv.ctypes.data if len(iv) else None, len(iv),
+                                       cands.ctypes.data, len(cands), C.byref(sp), C.byref(p),
+                                       out.ctypes.data, cig.ctypes.data, cigar_stride)
+    buf.check(rc)
+    cells = int(N.lib().esp_last_cells(buf.handle))
+    return out, cig[:len(reads) * cigar_stride].reshape(len(reads), cigar_stride), cells
+
+
+def synth_splice(seed: int, n_reads: int):
+    """Seeded splice workload (config 3):
+    (genome_arena, contigs, read_arena, reads, cands)."""
+    L = N.lib()
+    gb, rb, nc = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    rc = L.esp_synth_splice_size(seed, n_reads, C.byref(gb), C.byref(rb), C.byref(nc))
+    if rc:
+        raise N.EspError(rc, "esp_synth_splice_size")
+    garena = np.zeros(gb.value, np.uint8)
+    contigs = np.zeros(n_reads, CONTIG_DTYPE)
+    rarena = np.zeros(rb.value, np.uint8)
+    reads = np.zeros(n_reads, SPLICE_READ_DTYPE)
+    cands = np.zeros(nc.value, SPLICE_CAND_DTYPE)
+    rc = L.esp_synth_splice(seed, n_reads, garena.ctypes.data, gb.value, contigs.ctypes.data,
+                            rarena.ctypes.data, rb.value, reads.ctypes.data, cands.ctypes.data,
+                            nc.value)
+    if rc:
+        raise N.EspError(rc, "esp_synth_splice")
+    return garena, contigs, rarena, reads, cands

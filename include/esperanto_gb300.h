@@ -234,6 +234,119 @@ int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
                          const esp_n_interval *n_iv, uint64_t n_iv_count,
                          esp_myers_result *out);
 
+/* ---- resident genome: crates/map/src/fasta.rs Reference / Contig ----
+ *
+ * The genome stays in HBM as one 2-bit arena (MSB-first, the contig layout
+ * of fasta.rs:1-5); each contig is a base offset into it plus its length and
+ * its merged N intervals in contig coordinates (fasta.rs:62-75). */
+typedef struct {
+    uint64_t base;     /* arena base position of contig coordinate 0 */
+    uint32_t len;      /* contig length (bases) */
+    uint32_t n_first;  /* first N interval of this contig in the genome table */
+    uint32_t n_count;  /* number of its N intervals (sorted, merged) */
+    uint32_t pad;
+} esp_contig;
+
+typedef struct esp_genome esp_genome;
+
+/* Upload a genome (host arrays) to the handle's device.  The genome is
+ * immutable afterwards and may be shared by handles on the same device. */
+int esp_genome_create(esp_handle *h, const uint8_t *arena, uint64_t arena_bytes,
+                      const esp_contig *contigs, uint32_t n_contigs,
+                      const esp_n_interval *n_iv, uint64_t n_iv_count, esp_genome **out);
+int esp_genome_destroy(esp_genome *g);
+
+/* ---- splice-rescue flank DP: crates/map/src/split.rs ---- */
+
+/* crates/map/src/splice.rs:21-53 SpliceParams */
+typedef struct {
+    uint32_t min_intron;
+    uint32_t max_intron;
+    int32_t gt_ag_bonus;
+    int32_t gc_ag_bonus;
+    int32_t at_ac_bonus;
+    int32_t noncanonical_penalty;
+    int32_t known_bonus;
+    uint32_t refine_radius;
+} esp_splice_params;
+
+/* crates/map/src/gtf.rs:23-45 Junction and SpliceSignal */
+typedef struct {
+    uint32_t contig;
+    uint32_t start;        /* intron start (donor side) */
+    uint32_t end;          /* intron end (acceptor side, exclusive) */
+    int32_t minus_strand;
+} esp_junction;
+
+#define ESP_SIG_GTAG 0
+#define ESP_SIG_GCAG 1
+#define ESP_SIG_ATAC 2
+#define ESP_SIG_NONCANONICAL 3
+
+/* split.rs:120-132 RetryOutcome (the two CIGARs go to caller buffers) */
+typedef struct {
+    int32_t found;         /* Option::is_some */
+    uint32_t dro;
+    uint32_t left_win_lo;
+    int32_t total;
+    esp_extension left;
+    esp_extension right;
+} esp_retry_outcome;
+
+/* retry_tail_start (split.rs:150-223): retry the tail start +-5 around
+ * `tail_start` against junction `j`: per breakpoint, extend_hint the left
+ * segment in the window ending at the donor and the right segment in the
+ * window starting at the acceptor, gate both on coverage and seam anchoring,
+ * keep the best total (ties: lowest breakpoint).  `read` is ASCII. */
+int esp_retry_tail_start(esp_handle *h, const esp_genome *g, const uint8_t *read, size_t read_len,
+                         uint32_t tail_start, const esp_junction *j, int signal,
+                         uint32_t support, const esp_splice_params *sp,
+                         const esp_extend_params *params, esp_retry_outcome *out,
+                         uint32_t *left_cigar, uint32_t *right_cigar, uint32_t cigar_cap);
+
+/* Batch channel A (split.rs:468-570 with caller-supplied library
+ * candidates; one read per record, candidates in library order):
+ * retry every candidate, keep the best total (ties: first candidate), stitch
+ * left + N(intron) + right (build_rescue_ext, split.rs:227-240) and validate
+ * it (rescue_cigar_valid, split.rs:282-321). */
+typedef struct {
+    uint64_t read_pos;     /* base offset in the batch's read arena */
+    uint32_t read_len;
+    uint32_t tail_start;
+    uint32_t contig;
+    int32_t minus;         /* primary alignment strand is minus */
+    uint32_t cand_first;   /* first candidate of this read */
+    uint32_t cand_count;
+    uint32_t n_first;      /* read N intervals (relative to the read) */
+    uint32_t n_read;
+} esp_splice_read;
+
+typedef struct {
+    esp_junction j;
+    uint32_t support;      /* library support count */
+} esp_splice_cand;
+
+typedef struct {
+    int32_t found;
+    int32_t cand;          /* winning candidate (index within the read's list) */
+    uint32_t dro;
+    uint32_t pos;          /* left_win_lo + left.ref_start */
+    int32_t score;         /* retry total */
+    int32_t signal;
+    uint32_t n_ops;        /* spliced CIGAR length */
+    int32_t status;        /* ESP_OK, ESP_ECAP (a CIGAR did not fit), ESP_EDOMAIN */
+} esp_splice_result;
+
+int esp_batch_splice_host(esp_handle *h, const esp_genome *g, const esp_splice_read *reads,
+                          uint64_t n_reads, const uint8_t *read_arena, uint64_t read_arena_bytes,
+                          const esp_n_interval *read_n_iv, uint64_t read_n_iv_count,
+                          const esp_splice_cand *cands, uint64_t n_cands,
+                          const esp_splice_params *sp, const esp_extend_params *params,
+                          esp_splice_result *out, uint32_t *cigar, uint32_t cigar_stride);
+
+/* DP cells of the last batch splice call (both extension attempts counted). */
+uint64_t esp_last_cells(const esp_handle *h);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----
  *
  * esp_batch_run_band_noalloc: the same banded/full-matrix DP with traceback
@@ -283,6 +396,19 @@ int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
 int esp_synth_myers_size(uint64_t seed, uint64_t n_pairs, uint64_t *arena_bytes);
 int esp_synth_myers(uint64_t seed, uint64_t n_pairs, uint8_t *arena, uint64_t arena_bytes,
                     esp_myers_pair *pairs);
+
+/* Splice workload (config 3): per read a contig exon1(300) + intron
+ * (log-uniform 60..50,000, GT..AG planted) + exon2(300); the read is 150 bp
+ * across the junction split at U[20,130] with the Gotoh error model;
+ * candidates = the true junction plus decoys at every other GT within +-20
+ * of the donor and every other AG within +-20 of the acceptor (library
+ * order).  Sizes first, then fill caller memory. */
+int esp_synth_splice_size(uint64_t seed, uint64_t n_reads, uint64_t *genome_bytes,
+                          uint64_t *read_bytes, uint64_t *n_cands);
+int esp_synth_splice(uint64_t seed, uint64_t n_reads, uint8_t *genome_arena,
+                     uint64_t genome_bytes, esp_contig *contigs, uint8_t *read_arena,
+                     uint64_t read_bytes, esp_splice_read *reads, esp_splice_cand *cands,
+                     uint64_t n_cands);
 
 /* Number of device kernel launches the last batch call enqueued. */
 uint64_t esp_last_launch_count(const esp_handle *h);

@@ -1,0 +1,116 @@
+"""GPU parity for the splice-rescue flank DP (split.rs retry_tail_start and
+channel A) against the reference's known answers and the oracle."""
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import oracle as O  # noqa: E402
+from esperanto_gb300 import batch as B  # noqa: E402
+from esperanto_gb300 import split as S  # noqa: E402
+from golden_check import load  # noqa: E402
+
+
+def _oracle_retry(seq, read, ts, start, end, minus, sig, sup):
+    return O.retry_tail_start(O.Contig(seq), read, ts, start, end, minus, sig, sup)
+
+
+def _same(gpu, orc):
+    if orc is None:
+        return gpu is None
+    if gpu is None:
+        return False
+    return (gpu.dro, gpu.left_win_lo, gpu.total, gpu.left.key(), gpu.right.key()) == \
+        (orc.dro, orc.left_win_lo, orc.total, orc.left.key(), orc.right.key())
+
+
+@pytest.mark.parametrize("case", load()["retry"], ids=lambda c: c["name"])
+def test_retry_known_answers(case):
+    g = S.Genome.from_sequences([case["contig"]])
+    s, e, minus = case["junction"]
+    out = S.retry_tail_start(g, case["read"], case["tail_start"], S.Junction(0, s, e, minus),
+                             S.SIG_GTAG, case["support"])
+    exp = case["expect"]
+    if exp is None:
+        assert out is None
+    else:
+        assert out is not None
+        assert out.left.read_end == out.dro
+        assert out.right.read_start == exp["right_read_start"]
+        assert out.right.ref_start == exp["right_ref_start"]
+    orc = _oracle_retry(case["contig"], case["read"], case["tail_start"], s, e, minus,
+                        O.SIG_GTAG, case["support"])
+    assert _same(out, orc)
+
+
+def _rand_contig(rng, n, n_runs=0):
+    s = bytearray(rng.choice(b"ACGT") for _ in range(n))
+    for _ in range(n_runs):
+        a = rng.randrange(n)
+        for k in range(a, min(n, a + rng.randrange(1, 6))):
+            s[k] = ord("N")
+    return bytes(s)
+
+
+def test_retry_random_vs_oracle():
+    rng = random.Random(31)
+    for rep in range(120):
+        exon1, intron, exon2 = rng.randrange(10, 260), rng.randrange(30, 400), rng.randrange(10, 260)
+        seq = bytearray(_rand_contig(rng, exon1 + intron + exon2, n_runs=rep % 4))
+        d0, a0 = exon1, exon1 + intron
+        seq[d0:d0 + 2] = rng.choice([b"GT", b"GC", b"AT", b"CT", b"AA"])
+        seq[a0 - 2:a0] = rng.choice([b"AG", b"AC", b"GC", b"AT", b"TT"])
+        seq = bytes(seq)
+        L = rng.randrange(8, 200)
+        b = rng.randrange(1, L)
+        src = seq[max(0, d0 - b):d0] + seq[a0:a0 + (L - b)]
+        read = bytearray(src + b"A" * (L - len(src)))
+        for _ in range(rng.randrange(0, 4)):
+            read[rng.randrange(L)] = rng.choice(b"ACGTN")
+        read = bytes(read)
+        ts = max(0, b + rng.randrange(-4, 5))
+        start = d0 + rng.randrange(-3, 4)
+        end = a0 + rng.randrange(-3, 4)
+        minus = rng.random() < 0.3
+        sig, sup = rng.randrange(4), rng.randrange(0, 12)
+        g = S.Genome.from_sequences([seq])
+        got = S.retry_tail_start(g, read, ts, S.Junction(0, start, end, minus), sig, sup)
+        want = _oracle_retry(seq, read, ts, start, end, minus, sig, sup)
+        assert _same(got, want), rep
+
+
+def _oracle_channel_a(garena, contigs, rarena, reads, cands, r):
+    R = reads[r]
+    C = contigs[R["contig"]]
+    seq = B._ASCII[B.unpack_codes(garena, int(C["base"]), int(C["len"]))].tobytes()
+    read = B._ASCII[B.unpack_codes(rarena, int(R["read_pos"]), int(R["read_len"]))].tobytes()
+    cs = cands[int(R["cand_first"]):int(R["cand_first"]) + int(R["cand_count"])]
+    return O.channel_a(O.Contig(seq), read, int(R["tail_start"]), bool(R["minus"]),
+                       [(int(c["start"]), int(c["end"]), bool(c["minus_strand"])) for c in cs],
+                       [int(c["support"]) for c in cs])
+
+
+def test_config3_subset_channel_a():
+    garena, contigs, rarena, reads, cands = S.synth_splice(4, 600)
+    g = S.Genome(garena, contigs)
+    out, cig, cells = S.channel_a_batch(g, reads, rarena, cands)
+    assert cells > 0
+    assert (out["status"] == 0).all()
+    n_found = 0
+    for r in range(len(reads)):
+        want = _oracle_channel_a(garena, contigs, rarena, reads, cands, r)
+        o = out[r]
+        if want is None:
+            assert not o["found"], r
+            continue
+        n_found += 1
+        got = (int(o["cand"]), int(o["dro"]), int(o["pos"]), int(o["score"]), int(o["signal"]),
+               B.cigar_of(cig[r], int(o["n_ops"])))
+        assert got == (want.cand, want.dro, want.pos, want.score, want.signal, want.cigar), r
+    assert n_found > len(reads) // 2
