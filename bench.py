@@ -1,20 +1,26 @@
-"""Benchmark: batched banded Gotoh with traceback on one GB300 (or N replicas).
+"""Benchmark of the GB300 alignment inner loop (one JSON line on rank 0).
 
-Default workload = the mixed-length batched configuration: 4,194,304 read x
-window pairs, read length U[50,300], band half-width in {16,32,64,128} w.p.
-{.4,.3,.2,.1}, windows of read + 2*half, full CIGAR traceback (seeded
-synthetic data; the reference ships no dataset).  One step = one pass of the
-DP over the whole batch.  Metric: GCUPS (DP cells = sum over rows of the
-in-window width, crates/map/src/extend.rs:653-696).
+Default workload (config 2) = the mixed-length batched configuration:
+4,194,304 read x window pairs, read length U[50,300], band half-width in
+{16,32,64,128} w.p. {.4,.3,.2,.1}, windows of read + 2*half, banded affine DP
+with full CIGAR traceback, in one persistent length-binned launch.  Other
+workloads: --config 0 (plain 150 x 214 banded DP, 65,536 pairs), 1 (EA-Myers
+150-bp query vs 200-bp text, 1,048,576 pairs), 3 (splice-rescue flank DP,
+524,288 split reads over their candidate junctions), 4 (serve loop: see
+esperanto_gb300/serve.py).  All inputs are seeded synthetic data (the
+reference ships no dataset).
+
+One step = one pass of the hot path over the whole batch.  Metric: GCUPS,
+DP cells per second (cells = sum over rows of the in-window width of every
+DP attempt run, crates/map/src/extend.rs:653-696; Myers counts m*n).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--config 0|2] [--pairs P]
-
-Prints one JSON line on rank 0.
+                    [--config 0|1|2|3] [--pairs P]
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -28,10 +34,15 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-OPS_PER_CELL = 21  # integer ops of the cell recurrence as written in gotoh.cu (see DESIGN)
-INT_LANES_PER_SM = 128
-# Myers: 10 32-bit ops per 32-cell limb per text column (wide-word step)
+# Integer ops per cell of the DP recurrence as written in csrc/gotoh.cu
+# (E 3, F 3, key clears 3, LUT select 1, diag add 1, H max 3, H tag 1,
+# traceback bits 4, row-max key 2).
+OPS_PER_CELL = 21
+# Myers: 10 32-bit ops per 32-cell limb per text column (wide-word step).
 MYERS_OPS_PER_CELL = 10.0 / 32.0
+INT_LANES_PER_SM = 128
+DEFAULT_PAIRS = {0: 65536, 1: 1048576, 2: 4194304, 3: 524288}
+SEEDS = {0: 1, 1: 2, 2: 3, 3: 4}
 
 
 def load_peaks():
@@ -42,18 +53,9 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def workload_desc(config: int, n: int) -> str:
-    if config == 1:
-        return (f"bit-parallel EA-Myers infix_best_end: {n} pairs, 150-bp query vs 200-bp "
-                "text, 0-8 edits, 10% unrelated")
-    if config == 0:
-        return (f"plain banded Gotoh: {n} pairs, 150-bp reads vs 214-bp windows, "
-                "band half 32 at offset 32, traceback to CIGAR")
-    return (f"batched uneven Gotoh: {n} pairs, read U[50,300], half {{16,32,64,128}} "
-            "w.p. {.4,.3,.2,.1}, window read+2*half, traceback to CIGAR")
-
-
 class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
     def __init__(self):
         self.proc = None
         self.path = None
@@ -103,52 +105,264 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ---------------------------------------------------------------- workloads
+
+class Workload:
+    config = -1
+    dtype = "int16"
+    mode = ""
+    ops_per_cell = OPS_PER_CELL
+
+    def describe(self, n):
+        raise NotImplementedError
+
+
+class GotohWorkload(Workload):
+    """Configs 0 and 2: run_band with traceback over a pair batch."""
+
+    def __init__(self, config):
+        self.config = config
+        self.mode = "run_band"
+
+    def describe(self, n):
+        if self.config == 0:
+            return (f"plain banded Gotoh: {n} pairs, 150-bp reads vs 214-bp windows, "
+                    "band half 32 at offset 32, traceback to CIGAR")
+        return (f"batched uneven Gotoh: {n} pairs, read U[50,300], half {{16,32,64,128}} "
+                "w.p. {.4,.3,.2,.1}, window read+2*half, traceback to CIGAR")
+
+    def setup(self, seed, n, dev, buf, torch):
+        from esperanto_gb300 import _native as N
+        from esperanto_gb300 import batch as B
+        from esperanto_gb300.extend import ExtendParams
+        L = N.lib()
+        self.stride = 32
+        arena, pairs = B.synth_gotoh(seed, n, self.config)
+        self.cells = B.cells_of(pairs)
+        self.n = n
+        d_arena = torch.from_numpy(arena).to(dev)
+        d_pairs = torch.from_numpy(pairs.view(np.uint8)).to(dev)
+        d_out = torch.empty(n * B.EXT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        d_cig = torch.empty(n * self.stride, dtype=torch.int32, device=dev)
+        lim = N.BatchLimitsC(int(pairs["read_len"].max()), int(pairs["win_len"].max()),
+                             int(pairs["band_half"].max()))
+        p = ExtendParams()._c()
+        self._keep = (d_arena, d_pairs, d_out, d_cig, lim, p)
+
+        def step():
+            buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
+                                                d_arena.data_ptr(), arena.nbytes, None, 0,
+                                                C.byref(lim), C.byref(p), d_out.data_ptr(),
+                                                d_cig.data_ptr(), self.stride, None))
+        self.step = step
+        self.result_status = lambda: d_out.cpu().numpy().view(B.EXT_DTYPE)["status"]
+        pin_arena = torch.from_numpy(arena).pin_memory().numpy()
+        pin_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory().numpy()
+        out_pin = torch.empty(n * B.EXT_DTYPE.itemsize, dtype=torch.uint8).pin_memory().numpy()
+        cig_pin = torch.empty(n * self.stride, dtype=torch.int32).pin_memory().numpy()
+        self._pins = (pin_arena, pin_pairs, out_pin, cig_pin)
+
+        def e2e():
+            buf.check(L.esp_batch_extend_host(buf.handle, B.MODE_BAND, pin_pairs.ctypes.data, n,
+                                              pin_arena.ctypes.data, pin_arena.nbytes, None, 0,
+                                              C.byref(p), out_pin.ctypes.data,
+                                              cig_pin.ctypes.data, self.stride))
+        self.e2e_step = e2e
+        self.h2d = pin_arena.nbytes + pin_pairs.nbytes
+        self.d2h = out_pin.nbytes + cig_pin.nbytes
+        self.input_mb = arena.nbytes / 1e6
+
+    def cpu_reference(self, seed, sample, threads):
+        import oracle as O
+        from esperanto_gb300 import batch as B
+        O.build()
+        arena, pairs = B.synth_gotoh(seed, sample, self.config)
+        end = int((pairs["win_pos"] + pairs["win_len"]).max())
+        seq = B._ASCII[B.unpack_codes(arena, 0, end)]
+
+        def run():
+            t = time.perf_counter()
+            cells, _ = O.batch_extend(seq, pairs["read_pos"], pairs["read_len"], pairs["win_pos"],
+                                      pairs["win_len"], pairs["band_offset"], pairs["band_half"],
+                                      O.Params(), 0, threads)
+            return cells, time.perf_counter() - t
+        return run, f"{sample} pairs of the same workload per step"
+
+
+class MyersWorkload(Workload):
+    config = 1
+    dtype = "u32"
+    mode = "myers_ea::long::infix_best_end"
+    ops_per_cell = MYERS_OPS_PER_CELL
+
+    def describe(self, n):
+        return (f"bit-parallel EA-Myers infix_best_end: {n} pairs, 150-bp query vs 200-bp "
+                "text, 0-8 edits, 10% unrelated")
+
+    def setup(self, seed, n, dev, buf, torch):
+        from esperanto_gb300 import _native as N
+        from esperanto_gb300 import batch as B
+        L = N.lib()
+        arena, pairs = B.synth_myers(seed, n)
+        self.n = n
+        self.cells = int((pairs["read_len"].astype(np.int64) * pairs["text_len"]).sum())
+        d_arena = torch.from_numpy(arena).to(dev)
+        d_pairs = torch.from_numpy(pairs.view(np.uint8)).to(dev)
+        d_out = torch.empty(n * B.MYERS_RES_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        self._keep = (d_arena, d_pairs, d_out)
+
+        def step():
+            buf.check(L.esp_batch_myers_device(buf.handle, B.MYERS_BEST_END, d_pairs.data_ptr(),
+                                               n, 150, d_arena.data_ptr(), arena.nbytes, None, 0,
+                                               d_out.data_ptr(), None))
+        self.step = step
+        self.result_status = lambda: d_out.cpu().numpy().view(B.MYERS_RES_DTYPE)["status"]
+        pin_arena = torch.from_numpy(arena).pin_memory().numpy()
+        pin_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory().numpy()
+        out_pin = torch.empty(n * B.MYERS_RES_DTYPE.itemsize,
+                              dtype=torch.uint8).pin_memory().numpy()
+        self._pins = (pin_arena, pin_pairs, out_pin)
+
+        def e2e():
+            buf.check(L.esp_batch_myers_host(buf.handle, B.MYERS_BEST_END, pin_pairs.ctypes.data,
+                                             n, pin_arena.ctypes.data, pin_arena.nbytes, None, 0,
+                                             out_pin.ctypes.data))
+        self.e2e_step = e2e
+        self.h2d = pin_arena.nbytes + pin_pairs.nbytes
+        self.d2h = out_pin.nbytes
+        self.input_mb = arena.nbytes / 1e6
+
+    def cpu_reference(self, seed, sample, threads):
+        import oracle as O
+        from esperanto_gb300 import batch as B
+        O.build()
+        sample *= 16
+        arena, pairs = B.synth_myers(seed, sample)
+        end = int((pairs["text_pos"] + pairs["text_len"]).max())
+        seq = B._ASCII[B.unpack_codes(arena, 0, end)]
+
+        def run():
+            t = time.perf_counter()
+            cells, _, _ = O.batch_myers_best_end(seq, pairs["read_pos"], pairs["read_len"],
+                                                 pairs["text_pos"], pairs["text_len"], threads)
+            return cells, time.perf_counter() - t
+        return run, f"{sample} pairs of the same workload per step"
+
+
+class SpliceWorkload(Workload):
+    config = 3
+    mode = "split::channel_a (retry_tail_start per candidate)"
+
+    def describe(self, n):
+        return (f"splice-rescue flank DP: {n} 150-bp split reads (breakpoint U[20,130]), "
+                "300-bp exon flanks, intron log-U[60,50k], true + decoy GT/AG candidates, "
+                "11 breakpoints x 2 extend_hint per candidate")
+
+    def setup(self, seed, n, dev, buf, torch):
+        from esperanto_gb300 import _native as N
+        from esperanto_gb300 import split as S
+        from esperanto_gb300.extend import ExtendParams
+        L = N.lib()
+        garena, contigs, rarena, reads, cands = S.synth_splice(seed, n)
+        self.n = n
+        self.genome = S.Genome(garena, contigs, buf=buf)
+        sp, p = S.SpliceParams()._c(), ExtendParams()._c()
+        self.stride = 32
+        # one host-API pass gives the DP cell census of the batch
+        out, _, self.cells = S.channel_a_batch(self.genome, reads, rarena, cands,
+                                               cigar_stride=self.stride, buf=buf)
+        self.found = int(out["found"].sum())
+        d_reads = torch.from_numpy(reads.view(np.uint8)).to(dev)
+        d_arena = torch.from_numpy(rarena).to(dev)
+        d_cands = torch.from_numpy(cands.view(np.uint8)).to(dev)
+        d_out = torch.empty(n * S.SPLICE_RES_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        d_cig = torch.empty(n * self.stride, dtype=torch.int32, device=dev)
+        self._keep = (d_reads, d_arena, d_cands, d_out, d_cig, sp, p)
+
+        def step():
+            buf.check(L.esp_batch_splice_device(buf.handle, self.genome.handle,
+                                                d_reads.data_ptr(), n, 150, d_arena.data_ptr(),
+                                                rarena.nbytes, None, 0, d_cands.data_ptr(),
+                                                len(cands), C.byref(sp), C.byref(p),
+                                                d_out.data_ptr(), d_cig.data_ptr(), self.stride,
+                                                None))
+        self.step = step
+        self.result_status = lambda: d_out.cpu().numpy().view(S.SPLICE_RES_DTYPE)["status"]
+        pin = [torch.from_numpy(a.view(np.uint8) if a.dtype != np.uint8 else a).pin_memory()
+               .numpy() for a in (reads, rarena, cands)]
+        out_pin = torch.empty(n * S.SPLICE_RES_DTYPE.itemsize, dtype=torch.uint8).pin_memory().numpy()
+        cig_pin = torch.empty(n * self.stride, dtype=torch.int32).pin_memory().numpy()
+        self._pins = (pin, out_pin, cig_pin)
+
+        def e2e():
+            buf.check(L.esp_batch_splice_host(buf.handle, self.genome.handle, pin[0].ctypes.data,
+                                              n, pin[1].ctypes.data, pin[1].nbytes, None, 0,
+                                              pin[2].ctypes.data, len(cands), C.byref(sp),
+                                              C.byref(p), out_pin.ctypes.data,
+                                              cig_pin.ctypes.data, self.stride))
+        self.e2e_step = e2e
+        self.h2d = sum(a.nbytes for a in pin)
+        self.d2h = out_pin.nbytes + cig_pin.nbytes
+        self.input_mb = (garena.nbytes + rarena.nbytes) / 1e6
+        self.n_cands = len(cands)
+
+    def cpu_reference(self, seed, sample, threads):
+        import oracle as O
+        from esperanto_gb300 import batch as B
+        from esperanto_gb300 import split as S
+        O.build()
+        sample = max(64, sample // 16)
+        garena, contigs, rarena, reads, cands = S.synth_splice(seed, sample)
+        ra = B._ASCII[B.unpack_codes(rarena, 0, len(reads) * 150)]
+
+        def run():
+            t = time.perf_counter()
+            _, _, cells = O.batch_channel_a(garena, contigs, ra, reads["read_pos"], reads, cands,
+                                            threads)
+            return cells, time.perf_counter() - t
+        return run, f"{sample} split reads of the same workload per step"
+
+
+def make_workload(config):
+    if config == 1:
+        return MyersWorkload()
+    if config == 3:
+        return SpliceWorkload()
+    return GotohWorkload(config)
+
+
+# ---------------------------------------------------------------- main
+
 def dist_init(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl" if args.impl == "gpu" else "gloo"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl" if args.impl == "gpu" else "gloo")
     return rank, world, local
 
 
-def ascii_of_prefix(arena, pairs):
-    from esperanto_gb300 import batch as B
-    end = int((pairs["win_pos"] + pairs["win_len"]).max())
-    return B._ASCII[B.unpack_codes(arena, 0, end)]
-
-
-def cpu_reference(args, config, n_pairs, seed, threads):
-    """The reference's CPU path (restated scalar kernel) on a bounded sample."""
-    import oracle as O
-    from esperanto_gb300 import batch as B
-    sample = args.cpu_sample
-    if config == 1:
-        sample = sample * 16
-        arena, pairs = B.synth_myers(seed, sample)
-        end = int((pairs["text_pos"] + pairs["text_len"]).max())
-        seq = B._ASCII[B.unpack_codes(arena, 0, end)]
-        O.build()
-
-        def run_m():
-            t = time.perf_counter()
-            cells, _, _ = O.batch_myers_best_end(seq, pairs["read_pos"], pairs["read_len"],
-                                                 pairs["text_pos"], pairs["text_len"], threads)
-            return cells, time.perf_counter() - t
-        return run_m, sample
-    arena, pairs = B.synth_gotoh(seed, sample, config)
-    seq = ascii_of_prefix(arena, pairs)
-    O.build()
-
-    def run():
-        t = time.perf_counter()
-        cells, _ = O.batch_extend(seq, pairs["read_pos"], pairs["read_len"], pairs["win_pos"],
-                                  pairs["win_len"], pairs["band_offset"], pairs["band_half"],
-                                  O.Params(), 0, threads)
-        return cells, time.perf_counter() - t
-    return run, sample
+def reference_arm(args, wl, seed, threads, n_pairs):
+    run, sample = wl.cpu_reference(seed, args.cpu_sample, threads)
+    for _ in range(args.warmup):
+        run()
+    tot_cells, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        c, dt = run()
+        tot_cells += c
+        tot_t += dt
+    v = tot_cells / tot_t / 1e9
+    line = {"metric": "GCUPS", "value": v, "unit": "GCUPS", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic",
+            "config": {"workload": wl.describe(n_pairs), "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -157,7 +371,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2])
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3])
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -165,83 +379,31 @@ def main():
     args = ap.parse_args()
     rank, world, local = dist_init(args)
     config = args.config
-    n_pairs = args.pairs or {0: 65536, 1: 1048576, 2: 4194304}[config]
-    seed = {0: 1, 1: 2, 2: 3}[config] + 1000 * rank  # weak scaling: each rank its own batch
+    n_pairs = args.pairs or DEFAULT_PAIRS[config]
+    seed = SEEDS[config] + 1000 * rank  # weak scaling: each rank runs its own batch
     threads = os.cpu_count() or 1
+    wl = make_workload(config)
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        run, sample = cpu_reference(args, config, n_pairs, seed, threads)
-        for _ in range(args.warmup):
-            run()
-        tot_cells, tot_t = 0, 0.0
-        for _ in range(args.steps):
-            c, dt = run()
-            tot_cells += c
-            tot_t += dt
-        v = tot_cells / tot_t / 1e9
-        line = {"metric": "GCUPS", "value": v, "unit": "GCUPS", "impl": "reference",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None,
-                "dtype": "u32" if config == 1 else "int16",
-                "data": "synthetic", "config": {"workload": workload_desc(config, sample),
-                                                 "sample_of": n_pairs},
-                "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
-                                 "sample": f"{sample} pairs of the workload per step"},
-                "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
+        if rank == 0:
+            reference_arm(args, wl, seed, threads, n_pairs)
         return
 
     import torch
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     from esperanto_gb300 import _native as N
-    from esperanto_gb300 import batch as B
-    from esperanto_gb300.extend import ExtendBuffer, ExtendParams
-    import ctypes as C
-
-    buf = ExtendBuffer(local)
-    stride = 32
+    from esperanto_gb300.extend import ExtendBuffer
     L = N.lib()
+    buf = ExtendBuffer(local)
     stream = torch.cuda.ExternalStream(buf.stream_ptr())
-    p = ExtendParams()._c()
-    if config == 1:
-        arena, pairs = B.synth_myers(seed, n_pairs)
-        cells = int((pairs["read_len"].astype(np.int64) * pairs["text_len"]).sum())
-        res_dtype = B.MYERS_RES_DTYPE
-    else:
-        arena, pairs = B.synth_gotoh(seed, n_pairs, config)
-        cells = B.cells_of(pairs)
-        res_dtype = B.EXT_DTYPE
-    d_arena = torch.from_numpy(arena).to(f"cuda:{local}")
-    d_pairs = torch.from_numpy(pairs.view(np.uint8)).to(f"cuda:{local}")
-    d_out = torch.empty(n_pairs * res_dtype.itemsize, dtype=torch.uint8, device=f"cuda:{local}")
-    d_cig = torch.empty(max(1, n_pairs * stride if config != 1 else 1), dtype=torch.int32,
-                        device=f"cuda:{local}")
-    if config == 1:
-        def step():
-            rc = L.esp_batch_myers_device(buf.handle, B.MYERS_BEST_END, d_pairs.data_ptr(),
-                                          n_pairs, 150, d_arena.data_ptr(), arena.nbytes, None,
-                                          0, d_out.data_ptr(), None)
-            buf.check(rc)
-    else:
-        lim = N.BatchLimitsC(int(pairs["read_len"].max()), int(pairs["win_len"].max()),
-                             int(pairs["band_half"].max()))
+    wl.setup(seed, n_pairs, dev, buf, torch)
 
-        def step():
-            rc = L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n_pairs,
-                                           d_arena.data_ptr(), arena.nbytes, None, 0,
-                                           C.byref(lim), C.byref(p), d_out.data_ptr(),
-                                           d_cig.data_ptr(), stride, None)
-            buf.check(rc)
-
-    for _ in range(max(3, args.warmup)):
-        step()
+    warmup = max(3, args.warmup)
+    for _ in range(warmup):
+        wl.step()
     torch.cuda.synchronize()
-    out_host = d_out.cpu().numpy().view(res_dtype)
-    bad = int((out_host["status"] != 0).sum())
+    bad = int((wl.result_status() != 0).sum())
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -252,15 +414,15 @@ def main():
     with torch.cuda.stream(stream):
         evs[0].record(stream)
         for k in range(args.steps):
-            step()
+            wl.step()
             evs[k + 1].record(stream)
     torch.cuda.synchronize()
     clocks = clk.stop(local)
     per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     ms = sum(per_step) / args.steps
     launches = int(L.esp_last_launch_count(buf.handle)) * args.steps
-    tmax = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
-    tcells = torch.tensor([float(cells)], dtype=torch.float64, device=f"cuda:{local}")
+    tmax = torch.tensor([ms], dtype=torch.float64, device=dev)
+    tcells = torch.tensor([float(wl.cells)], dtype=torch.float64, device=dev)
     if world > 1:
         import torch.distributed as dist
         dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
@@ -268,73 +430,57 @@ def main():
     ms_max = float(tmax.item())
     value = float(tcells.item()) / (ms_max / 1e3) / 1e9
 
-    # end to end: host arrays (pinned) through the host C-ABI call
-    pin_arena = torch.from_numpy(arena).pin_memory().numpy()
-    pin_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory().numpy()
-    out_pin = torch.empty(n_pairs * res_dtype.itemsize, dtype=torch.uint8).pin_memory().numpy()
-    cig_pin = torch.empty(n_pairs * stride if config != 1 else 1,
-                          dtype=torch.int32).pin_memory().numpy()
-
-    def e2e_step():
-        if config == 1:
-            rc = L.esp_batch_myers_host(buf.handle, B.MYERS_BEST_END, pin_pairs.ctypes.data,
-                                        n_pairs, pin_arena.ctypes.data, pin_arena.nbytes, None,
-                                        0, out_pin.ctypes.data)
-        else:
-            rc = L.esp_batch_extend_host(buf.handle, B.MODE_BAND, pin_pairs.ctypes.data,
-                                         n_pairs, pin_arena.ctypes.data, pin_arena.nbytes,
-                                         None, 0, C.byref(p), out_pin.ctypes.data,
-                                         cig_pin.ctypes.data, stride)
-        buf.check(rc)
-    e2e_step()
+    wl.e2e_step()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        e2e_step()
+        wl.e2e_step()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    e2e_val = cells / e2e_s / 1e9
-    h2d = pin_arena.nbytes + pin_pairs.nbytes
-    d2h = out_pin.nbytes + (cig_pin.nbytes if config != 1 else 0)
-
+    e2e_val = wl.cells / e2e_s / 1e9
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     if rank != 0:
         return
+
     peaks, src = load_peaks()
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    mhz = (clocks or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    peak_ops = sm_count * INT_LANES_PER_SM * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    ops_per_cell = MYERS_OPS_PER_CELL if config == 1 else OPS_PER_CELL
-    achieved_ops = cells * ops_per_cell / (ms / 1e3) / 1e12
+    max_mhz = peaks.get("sm_max_mhz", 2070.0)
+    peak_ops = sm_count * INT_LANES_PER_SM * max_mhz * 1e6 / 1e12
+    achieved_ops = wl.cells * wl.ops_per_cell / (ms / 1e3) / 1e12
     cpu = None
     if not args.no_cpu_baseline:
-        run, sample = cpu_reference(args, config, n_pairs, seed, threads)
+        run, sample = wl.cpu_reference(seed, args.cpu_sample, threads)
         run()
         c, dt = run()
         cpu = {"value": c / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
-               "sample": f"{sample} pairs of the same workload, restated scalar kernel "
-                         f"(run_band<i16>, what the reference runs on aarch64)"}
+               "sample": sample + " (oracle restatement of the reference's scalar kernel, "
+                                  "the code path the reference runs on aarch64)"}
     line = {
         "metric": "GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world,
-        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_max,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32" if config == 1 else "int16", "data": "synthetic",
-        "config": {"workload": workload_desc(config, n_pairs), "pairs": n_pairs,
-                   "cells_per_step": cells,
-                   "mode": "myers_ea::long::infix_best_end" if config == 1 else "run_band",
-                   "l2": "inputs larger than L2 (arena %.0f MB + traceback scratch)"
-                         % (arena.nbytes / 1e6)},
+        "steps": args.steps, "warmup": warmup, "ms_per_step": ms_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype,
+        "data": "synthetic",
+        "config": {"workload": wl.describe(n_pairs), "pairs": n_pairs,
+                   "cells_per_step": wl.cells, "mode": wl.mode,
+                   "l2": "inputs larger than L2 (%.0f MB of sequence + DP scratch)"
+                         % wl.input_mb},
         "pairs_per_s": n_pairs * world / (ms_max / 1e3),
         "bad_status": bad,
         "gpu_launches": launches,
         "roofline": {"bound": "int_alu", "achieved": achieved_ops, "peak": peak_ops,
                      "unit": "Tops/s", "frac": achieved_ops / peak_ops, "traffic": None,
-                     "peak_source": f"nominal: {sm_count} SMs x {INT_LANES_PER_SM} INT32 lanes x "
-                                    f"{peaks.get('sm_max_mhz', 2070.0):.0f} MHz ({src} clock)",
-                     "ops_per_cell": ops_per_cell},
-        "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                     "peak_source": f"nominal: {sm_count} SMs x {INT_LANES_PER_SM} INT32 lanes "
+                                    f"x {max_mhz:.0f} MHz ({src} max clock)",
+                     "ops_per_cell": wl.ops_per_cell},
+        "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(wl.h2d),
+                "d2h_bytes_per_step": int(wl.d2h)},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "per_step_ms": per_step,
     }
+    if config == 3:
+        line["config"]["candidates"] = wl.n_cands
+        line["config"]["rescued"] = wl.found
     print(json.dumps(line), flush=True)
 
 

@@ -151,6 +151,10 @@ def lib():
     L.esp_batch_splice_host.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64,
                                         vp, C.c_uint64, C.POINTER(SpliceParamsC),
                                         C.POINTER(ExtendParamsC), vp, vp, C.c_uint32]
+    L.esp_batch_splice_device.argtypes = [vp, vp, vp, C.c_uint64, C.c_uint32, vp, C.c_uint64,
+                                          vp, C.c_uint64, vp, C.c_uint64,
+                                          C.POINTER(SpliceParamsC), C.POINTER(ExtendParamsC),
+                                          vp, vp, C.c_uint32, vp]
     L.esp_last_cells.argtypes = [vp]
     L.esp_last_cells.restype = C.c_uint64
     L.esp_synth_splice_size.argtypes = [C.c_uint64, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3

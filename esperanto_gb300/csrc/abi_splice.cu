@@ -300,4 +300,26 @@ int esp_batch_splice_host(esp_handle *h, const esp_genome *g, const esp_splice_r
     return ESP_OK;
 }
 
+int esp_batch_splice_device(esp_handle *h, const esp_genome *g, const esp_splice_read *reads,
+                            uint64_t n_reads, uint32_t max_read_len, const uint8_t *read_arena,
+                            uint64_t read_arena_bytes, const esp_n_interval *read_n_iv,
+                            uint64_t read_n_iv_count, const esp_splice_cand *cands,
+                            uint64_t n_cands, const esp_splice_params *sp,
+                            const esp_extend_params *params, esp_splice_result *out,
+                            uint32_t *cigar, uint32_t cigar_stride, void *stream) {
+    if (!h || !g || !sp || !params || !out || (n_reads && (!reads || !read_arena)) ||
+        (n_cands && !cands))
+        return fail(h, ESP_EINVAL, "null argument");
+    if (max_read_len < 1 || max_read_len > 32767) return fail(h, ESP_EDOMAIN, "read length");
+    esp::GotohConst K;
+    if (esp::make_gotoh_const(*params, K) != ESP_OK)
+        return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
+    CK(h, cudaSetDevice(h->device));
+    SpliceBufs B;
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    return enqueue_splice(h, g, reads, n_reads, max_read_len, read_arena, read_arena_bytes,
+                          read_n_iv_count ? read_n_iv : nullptr, read_n_iv_count, cands, n_cands,
+                          *sp, K, out, cigar, cigar_stride, st, false, 0, B);
+}
+
 }  // extern "C"

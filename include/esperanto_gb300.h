@@ -344,6 +344,16 @@ int esp_batch_splice_host(esp_handle *h, const esp_genome *g, const esp_splice_r
                           const esp_splice_params *sp, const esp_extend_params *params,
                           esp_splice_result *out, uint32_t *cigar, uint32_t cigar_stride);
 
+/* Device-resident variant (all pointers device memory; asynchronous on
+ * `stream`, NULL = handle stream).  Reads may not exceed max_read_len. */
+int esp_batch_splice_device(esp_handle *h, const esp_genome *g, const esp_splice_read *reads,
+                            uint64_t n_reads, uint32_t max_read_len, const uint8_t *read_arena,
+                            uint64_t read_arena_bytes, const esp_n_interval *read_n_iv,
+                            uint64_t read_n_iv_count, const esp_splice_cand *cands,
+                            uint64_t n_cands, const esp_splice_params *sp,
+                            const esp_extend_params *params, esp_splice_result *out,
+                            uint32_t *cigar, uint32_t cigar_stride, void *stream);
+
 /* DP cells of the last batch splice call (both extension attempts counted). */
 uint64_t esp_last_cells(const esp_handle *h);
 

@@ -145,6 +145,8 @@ def lib():
         L.orc_batch_myers_best_end.argtypes = [C.c_void_p] * 5 + [i64, C.c_int, C.c_void_p,
                                                                    C.c_void_p]
         L.orc_batch_myers_best_end.restype = i64
+        L.orc_batch_channel_a.argtypes = [C.c_void_p] * 13 + [i64, C.c_int, C.c_void_p,
+                                                               C.c_void_p, C.c_void_p]
         L.free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -531,3 +533,25 @@ def batch_myers_best_end(seqs, read_off, read_len, text_off, text_len, threads: 
     if cells < 0:
         raise OracleError(f"orc_batch_myers_best_end returned {cells}")
     return int(cells), dist, end
+
+
+def batch_channel_a(garena, contigs, read_ascii, read_off, reads, cands, threads: int):
+    """Channel A per read with `threads` workers (plus strand, defaults).
+    Returns (found, score, dp_cells)."""
+    import numpy as np
+    n = len(reads)
+    keep = [np.ascontiguousarray(a) for a in (
+        garena, contigs["base"].astype(np.uint64), contigs["len"].astype(np.uint32), read_ascii,
+        read_off.astype(np.uint64), reads["read_len"].astype(np.uint32),
+        reads["tail_start"].astype(np.uint32), reads["contig"].astype(np.uint32),
+        reads["cand_first"].astype(np.uint32), reads["cand_count"].astype(np.uint32),
+        cands["start"].astype(np.uint32), cands["end"].astype(np.uint32),
+        cands["support"].astype(np.uint32))]
+    found = np.zeros(n, np.int32)
+    score = np.zeros(n, np.int32)
+    cells = C.c_int64()
+    rc = lib().orc_batch_channel_a(*[a.ctypes.data for a in keep], n, threads,
+                                   found.ctypes.data, score.ctypes.data, C.byref(cells))
+    if rc != 0:
+        raise OracleError(f"orc_batch_channel_a returned {rc}")
+    return found, score, cells.value

@@ -8,6 +8,8 @@
 #include "esp_oracle.h"
 
 #include <pthread.h>
+
+extern _Thread_local int64_t orc_tls_cells;
 #include <stdlib.h>
 #include <string.h>
 
@@ -171,4 +173,87 @@ int64_t orc_batch_myers_best_end(const uint8_t *seqs, const uint64_t *read_off,
     free(tid);
     free(jobs);
     return rc != ORC_OK ? rc : cells;
+}
+
+/* ---- channel A over a batch (CPU baseline of the splice configuration) ---- */
+typedef struct {
+    const uint8_t *garena;
+    const uint64_t *cbase;
+    const uint32_t *clen;
+    const uint8_t *reads;       /* ASCII, concatenated */
+    const uint64_t *read_off;
+    const uint32_t *read_len;
+    const uint32_t *tail_start;
+    const uint32_t *contig;
+    const uint32_t *cand_first;
+    const uint32_t *cand_count;
+    const uint32_t *cstart, *cend, *csupport;
+    int64_t lo, hi;
+    int32_t *found, *score;
+    int rc;
+    int64_t cells;
+} ca_job;
+
+static void *ca_worker(void *arg) {
+    ca_job *jb = (ca_job *)arg;
+    orc_splice_params sp;
+    orc_splice_params_default(&sp);
+    orc_params p = {2, -4, 4, 2, ORC_EDIT_OFF};
+    jb->rc = ORC_OK;
+    int64_t c0 = orc_tls_cells;
+    for (int64_t r = jb->lo; r < jb->hi; r++) {
+        uint32_t c = jb->contig[r];
+        orc_contig ctg = {jb->clen[c], jb->garena + (jb->cbase[c] >> 2), NULL, 0};
+        uint32_t n = jb->cand_count[r], f = jb->cand_first[r];
+        orc_junction *js = (orc_junction *)malloc((n ? n : 1) * sizeof(orc_junction));
+        for (uint32_t k = 0; k < n; k++) js[k] = (orc_junction){jb->cstart[f + k], jb->cend[f + k], 0};
+        uint32_t ops[1024];
+        orc_rescue out = {0};
+        out.ops = ops;
+        out.cap = 1024;
+        int rc = orc_channel_a(&ctg, jb->reads + jb->read_off[r], jb->read_len[r],
+                               jb->tail_start[r], 0, js, jb->csupport + f, n, &sp, &p, &out);
+        free(js);
+        if (rc != ORC_OK) { jb->rc = rc; break; }
+        jb->found[r] = out.found;
+        jb->score[r] = out.score;
+    }
+    jb->cells = orc_tls_cells - c0;
+    return NULL;
+}
+
+int orc_batch_channel_a(const uint8_t *garena, const uint64_t *cbase, const uint32_t *clen,
+                        const uint8_t *reads, const uint64_t *read_off, const uint32_t *read_len,
+                        const uint32_t *tail_start, const uint32_t *contig,
+                        const uint32_t *cand_first, const uint32_t *cand_count,
+                        const uint32_t *cstart, const uint32_t *cend, const uint32_t *csupport,
+                        int64_t n_reads, int threads, int32_t *found, int32_t *score,
+                        int64_t *cells) {
+    if (threads < 1) threads = 1;
+    if (threads > 1024) threads = 1024;
+    pthread_t *tid = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+    ca_job *jobs = (ca_job *)calloc((size_t)threads, sizeof(ca_job));
+    if (!tid || !jobs) { free(tid); free(jobs); return ORC_ENOMEM; }
+    int64_t chunk = (n_reads + threads - 1) / threads;
+    for (int t = 0; t < threads; t++) {
+        ca_job *jb = &jobs[t];
+        *jb = (ca_job){garena, cbase, clen, reads, read_off, read_len, tail_start, contig,
+                       cand_first, cand_count, cstart, cend, csupport, 0, 0, found, score, 0,
+                       0};
+        jb->lo = (int64_t)t * chunk;
+        jb->hi = jb->lo + chunk < n_reads ? jb->lo + chunk : n_reads;
+        if (jb->lo > jb->hi) jb->lo = jb->hi;
+        pthread_create(&tid[t], NULL, ca_worker, jb);
+    }
+    int rc = ORC_OK;
+    int64_t total = 0;
+    for (int t = 0; t < threads; t++) {
+        pthread_join(tid[t], NULL);
+        if (jobs[t].rc != ORC_OK) rc = jobs[t].rc;
+        total += jobs[t].cells;
+    }
+    if (cells) *cells = total;
+    free(tid);
+    free(jobs);
+    return rc;
 }

@@ -13,6 +13,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* DP cells computed by run_band on this thread (rows 1..m window widths);
+ * read by the batch drivers for the CPU-baseline cell census. */
+_Thread_local int64_t orc_tls_cells = 0;
+
 /* extend.rs:601-604 */
 enum { H_DIAG = 0, H_FROM_E = 1, H_FROM_F = 2, H_START = 3 };
 
@@ -440,6 +444,7 @@ int orc_run_band(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
         plo = lo;
         phi = hi;
     }
+    orc_tls_cells += (int64_t)(flat_len - rows[0].len);
     int rcode = finish_extension(m, &core, rows, flat, read_codes, ref_codes, n, best_i,
                                  best_j, out);
     free(buf);
