@@ -323,6 +323,52 @@ class SpliceWorkload(Workload):
         return run, f"{sample} split reads of the same workload per step"
 
 
+def serve_bench(args):
+    """Config 4: the serving loop on a 3.1-Gbp resident genome.  Measures the
+    saturated throughput (closed loop), then Poisson arrivals of 1k-64k-read
+    requests (log-uniform) at 70% and 80% of it, reporting p50/p99 latency."""
+    import torch
+    from esperanto_gb300 import serve as SV
+    from esperanto_gb300.extend import ExtendBuffer
+    from esperanto_gb300.split import Genome
+    torch.cuda.set_device(0)
+    buf = ExtendBuffer(0)
+    t0 = time.perf_counter()
+    garena, contigs = SV.synth_genome(5, args.genome_bases, 24)
+    genome = Genome(garena, contigs, buf=buf)
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(5)
+    sizes = np.exp(rng.uniform(np.log(1000), np.log(65536), args.pool)).astype(int)
+    pool = [SV.synth_request(5, k, garena, contigs, int(n)) for k, n in enumerate(sizes)]
+    srv = SV.Server(genome, n_streams=args.streams, max_reads=65536, mem_budget=16 << 30)
+    # warm up every slot
+    for t in [srv.submit(*pool[k % len(pool)]) for k in range(2 * args.streams)]:
+        srv.wait(t)
+    lat, pairs, wall, tks = SV.run_load(srv, pool, 0, args.serve_seconds / 2, closed_loop=True)
+    peak = pairs / wall
+    cells = sum(SV.hint_cells(t.reads, contigs, t.out) for t in tks)
+    peak_gcups = cells / wall / 1e9
+    res = {}
+    for frac in (0.7, 0.8):
+        lat, pairs, wall, tks = SV.run_load(srv, pool, frac * peak, args.serve_seconds, seed=7)
+        res[f"{int(frac * 100)}pct"] = {
+            "offered_pairs_per_s": frac * peak, "achieved_pairs_per_s": pairs / wall,
+            "requests": len(lat), "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max())}
+    srv.destroy()
+    r70 = res["70pct"]
+    line = {"metric": "serve p99 latency at 70% of peak load", "value": r70["p99_ms"],
+            "unit": "ms", "n_gpus": 1, "higher_is_better": False, "data": "synthetic",
+            "dtype": "int16", "vs_baseline": None,
+            "config": {"workload": "serve loop: %.2f-Gbp resident genome (24 contigs), Poisson "
+                                   "requests of 1k-64k reads (log-uniform), 2x150 PE, windows "
+                                   "read +- 32, extend_hint policy" % (args.genome_bases / 1e9),
+                       "streams": args.streams, "request_pool": args.pool},
+            "peak_pairs_per_s": peak, "peak_gcups": peak_gcups, "load": res,
+            "setup_s": setup_s}
+    print(json.dumps(line), flush=True)
+
+
 def make_workload(config):
     if config == 1:
         return MyersWorkload()
@@ -371,7 +417,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3])
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4])
+    ap.add_argument("--genome-bases", type=int, default=3_100_000_000)
+    ap.add_argument("--pool", type=int, default=48)
+    ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -379,6 +429,10 @@ def main():
     args = ap.parse_args()
     rank, world, local = dist_init(args)
     config = args.config
+    if config == 4:
+        if rank == 0 and args.impl == "gpu":
+            serve_bench(args)
+        return
     n_pairs = args.pairs or DEFAULT_PAIRS[config]
     seed = SEEDS[config] + 1000 * rank  # weak scaling: each rank runs its own batch
     threads = os.cpu_count() or 1

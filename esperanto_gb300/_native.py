@@ -79,6 +79,18 @@ class RetryOutcomeC(C.Structure):
                 ("total", C.c_int32), ("left", ExtensionC), ("right", ExtensionC)]
 
 
+class ServeRequestC(C.Structure):
+    _fields_ = [("read_arena", C.c_void_p), ("read_arena_bytes", C.c_uint64),
+                ("reads", C.c_void_p), ("n_reads", C.c_uint64), ("out", C.c_void_p),
+                ("cigar", C.c_void_p), ("cigar_stride", C.c_uint32)]
+
+
+class ServerConfigC(C.Structure):
+    _fields_ = [("n_streams", C.c_uint32), ("max_reads", C.c_uint32),
+                ("max_read_len", C.c_uint32), ("max_win_len", C.c_uint32),
+                ("mem_budget_bytes", C.c_uint64)]
+
+
 class BatchLimitsC(C.Structure):
     _fields_ = [("max_read_len", C.c_uint32), ("max_win_len", C.c_uint32),
                 ("max_half", C.c_int32)]
@@ -155,6 +167,16 @@ def lib():
                                           vp, C.c_uint64, vp, C.c_uint64,
                                           C.POINTER(SpliceParamsC), C.POINTER(ExtendParamsC),
                                           vp, vp, C.c_uint32, vp]
+    L.esp_server_create.argtypes = [vp, C.POINTER(ExtendParamsC), C.POINTER(ServerConfigC),
+                                    C.c_int, C.POINTER(vp)]
+    L.esp_server_submit.argtypes = [vp, C.POINTER(ServeRequestC), C.POINTER(C.c_uint64)]
+    L.esp_server_wait.argtypes = [vp, C.c_uint64, C.c_int, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_double)]
+    L.esp_server_close.argtypes = [vp]
+    L.esp_server_destroy.argtypes = [vp]
+    L.esp_synth_genome.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, vp, C.c_uint64, vp]
+    L.esp_synth_serve_reads.argtypes = [C.c_uint64, C.c_uint64, vp, vp, C.c_uint32, C.c_uint64,
+                                        vp, C.c_uint64, vp]
     L.esp_last_cells.argtypes = [vp]
     L.esp_last_cells.restype = C.c_uint64
     L.esp_synth_splice_size.argtypes = [C.c_uint64, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3

@@ -101,6 +101,31 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
 
 
 
+int reserve_dp(esp_handle *h, uint64_t max_pairs, uint32_t max_m, uint32_t max_n) {
+    Limits L1, L2;
+    add_limits(L1, max_m, max_n, 30);
+    add_limits(L2, max_m, max_n, -1);
+    uint64_t tbw = std::max(L1.tb_words, L2.tb_words), rbw = std::max(L1.rb_words, L2.rb_words);
+    uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
+    if (h->variant < 0) {
+        const char *v = getenv("ESP_GOTOH_VARIANT");
+        h->variant = (v && *v == '0') ? 0 : 1;
+    }
+    if (h->gotoh_bps[h->variant] == 0)
+        h->gotoh_bps[h->variant] = esp::gotoh_blocks_per_sm(128, h->variant);
+    uint64_t warps = std::min<uint64_t>((uint64_t)h->num_sms * h->gotoh_bps[h->variant] * 4,
+                                        (max_pairs + 31) / 32);
+    warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes));
+    warps = (warps + 3) / 4 * 4;
+    int rc;
+    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * tbw * 32 * 4)) != ESP_OK) return rc;
+    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * rbw * 32 * 4)) != ESP_OK) return rc;
+    if ((rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, max_pairs * 4)) != ESP_OK) return rc;
+    if ((rc = grow_device(h, (void **)&h->d_hist, &h->d_hist_cap, esp::bin_scratch_bytes())) != ESP_OK)
+        return rc;
+    return grow_device(h, (void **)&h->d_order, &h->d_order_cap, max_pairs * 4);
+}
+
 extern "C" {
 
 int esp_create(esp_handle **out, int device) {

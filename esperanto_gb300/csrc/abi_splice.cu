@@ -128,6 +128,7 @@ int esp_genome_create(esp_handle *h, const uint8_t *arena, uint64_t arena_bytes,
     g->arena_bytes = arena_bytes;
     g->contigs.assign(contigs, contigs + n_contigs);
     g->n_iv = n_iv_count;
+    if (n_iv_count) g->h_iv.assign(n_iv, n_iv + n_iv_count);
     cudaError_t e = cudaMalloc((void **)&g->d_arena, arena_bytes + 16);
     if (e == cudaSuccess) e = cudaMalloc((void **)&g->d_contigs, std::max<size_t>(1, n_contigs) * sizeof(esp_contig));
     if (e == cudaSuccess) e = cudaMalloc((void **)&g->d_iv, std::max<size_t>(1, n_iv_count) * sizeof(esp_n_interval));

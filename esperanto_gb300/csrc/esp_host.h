@@ -169,4 +169,9 @@ struct esp_genome {
     std::vector<esp_contig> contigs;
     esp_n_interval *d_iv = nullptr;
     uint64_t n_iv = 0;
+    std::vector<esp_n_interval> h_iv;  // host copy (serve-loop window clipping)
 };
+
+// Grow a handle's DP scratch once for batches of up to max_pairs pairs of
+// at most max_m x max_n in extend_hint mode (abi.cu).
+int reserve_dp(esp_handle *h, uint64_t max_pairs, uint32_t max_m, uint32_t max_n);

@@ -387,4 +387,77 @@ int esp_synth_splice(uint64_t seed, uint64_t n_reads, uint8_t *genome_arena,
     return ESP_OK;
 }
 
+// Config 4 (serve): uniform-ACGT genome, equal contigs starting on whole
+// bytes; every 4 bases are one uniformly random byte.
+int esp_synth_genome(uint64_t seed, uint64_t total_bases, uint32_t n_contigs, uint8_t *arena,
+                     uint64_t arena_bytes, esp_contig *contigs) {
+    if (!arena || !contigs || n_contigs == 0) return ESP_EINVAL;
+    uint64_t stride = ((total_bases + n_contigs - 1) / n_contigs + 3) / 4 * 4;
+    if (stride > 0xffffffffull) return ESP_EDOMAIN;
+    uint64_t bytes = (stride * n_contigs) / 4;
+    if (bytes + 16 > arena_bytes) return ESP_EINVAL;
+    const uint64_t chunk = 1 << 20;
+    uint64_t nchunks = (bytes + chunk - 1) / chunk;
+    parallel_for(nchunks, [&](uint64_t c) {
+        Rng r(pair_seed(seed ^ 0x47454E4Full, c));
+        uint64_t lo = c * chunk, hi = std::min(bytes, lo + chunk);
+        for (uint64_t b = lo; b < hi; b += 8) {
+            uint64_t v = r.next();
+            for (uint64_t k = 0; k < 8 && b + k < hi; k++) arena[b + k] = (uint8_t)(v >> (8 * k));
+        }
+    });
+    memset(arena + bytes, 0, arena_bytes - bytes);
+    for (uint32_t c = 0; c < n_contigs; c++) {
+        uint64_t base = (uint64_t)c * stride;
+        uint64_t len = base >= total_bases ? 0 : std::min<uint64_t>(stride, total_bases - base);
+        contigs[c].base = base;
+        contigs[c].len = (uint32_t)len;
+        contigs[c].n_first = 0;
+        contigs[c].n_count = 0;
+        contigs[c].pad = 0;
+    }
+    return ESP_OK;
+}
+
+// Serve requests: fragment f = reads 2f, 2f+1 (mates, 150 bp, insert
+// 250..450), both as forward-strand reads of the genome with the Gotoh error
+// model; window = read position -32 .. +182 (read + 2 x 32), hint offset 32.
+int esp_synth_serve_reads(uint64_t seed, uint64_t request, const uint8_t *genome_arena,
+                          const esp_contig *contigs, uint32_t n_contigs, uint64_t n_reads,
+                          uint8_t *read_arena, uint64_t read_arena_bytes, esp_serve_read *reads) {
+    if (!genome_arena || !contigs || !read_arena || !reads || n_contigs == 0) return ESP_EINVAL;
+    if ((n_reads * 150 + 3) / 4 + 16 > read_arena_bytes) return ESP_EINVAL;
+    memset(read_arena, 0, read_arena_bytes);
+    uint64_t frags = (n_reads + 1) / 2;
+    parallel_for(frags, [&](uint64_t f) {
+        Rng r(pair_seed(seed ^ (0x5345525645ull + request * 0x9E3779B97F4A7C15ull), f));
+        uint32_t c = r.below(n_contigs);
+        const esp_contig &C = contigs[c];
+        uint32_t insert = 250 + r.below(201);
+        uint32_t span = insert + 32 + 32 + 200;
+        uint32_t p1 = C.len > span ? 32 + r.below(C.len - span) : 32;
+        uint32_t pos[2] = {p1, p1 + insert - 150};
+        uint8_t win[200], rd[150];
+        for (int m = 0; m < 2; m++) {
+            uint64_t i = 2 * f + m;
+            if (i >= n_reads) break;
+            for (int k = 0; k < 200; k++) {
+                uint64_t gp = C.base + pos[m] + k;
+                win[k] = (uint8_t)((genome_arena[gp >> 2] >> (6 - 2 * (gp & 3))) & 3);
+            }
+            derive_read(r, win, 200, 0, 150, rd);
+            for (int k = 0; k < 150; k++) put2(read_arena, i * 150 + k, rd[k]);
+            esp_serve_read &R = reads[i];
+            R.read_pos = i * 150;
+            R.read_len = 150;
+            R.contig = c;
+            R.win_start = pos[m] >= 32 ? pos[m] - 32 : 0;
+            R.win_len = 214;
+            R.hint_offset = (int32_t)(pos[m] - R.win_start);
+            R.pad = 0;
+        }
+    });
+    return ESP_OK;
+}
+
 }  // extern "C"

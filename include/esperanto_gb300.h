@@ -357,6 +357,61 @@ int esp_batch_splice_device(esp_handle *h, const esp_genome *g, const esp_splice
 /* DP cells of the last batch splice call (both extension attempts counted). */
 uint64_t esp_last_cells(const esp_handle *h);
 
+/* ---- serving loop (new): continuous batching over a resident genome ----
+ *
+ * A server owns `n_streams` in-flight slots, each a CUDA stream with its own
+ * pre-sized DP scratch.  Submitted requests wait in a FIFO; a native worker
+ * thread admits the head request to an idle slot as soon as the slot and the
+ * device-memory budget (DP scratch, dominated by traceback words) allow,
+ * builds each read's candidate window from the resident genome, runs the
+ * extend_hint policy on the slot's stream and copies results back, so
+ * requests that arrive while others run are admitted as slots free up and
+ * their work overlaps on the device.  Results of a request do not depend on
+ * what else is in flight. */
+typedef struct {
+    uint64_t read_pos;     /* base offset in the request's read arena */
+    uint32_t read_len;
+    uint32_t contig;
+    uint32_t win_start;    /* candidate window [win_start, win_start + win_len) */
+    uint32_t win_len;      /* clipped to the contig */
+    int32_t hint_offset;   /* DiagHint.offset within the window */
+    uint32_t pad;
+} esp_serve_read;
+
+typedef struct {
+    const uint8_t *read_arena; /* host, 2-bit packed; kept alive until completion */
+    uint64_t read_arena_bytes;
+    const esp_serve_read *reads;
+    uint64_t n_reads;
+    esp_extension *out;        /* host results, n_reads records */
+    uint32_t *cigar;           /* host, n_reads * cigar_stride ops */
+    uint32_t cigar_stride;
+} esp_serve_request;
+
+typedef struct {
+    uint32_t n_streams;        /* in-flight slots (default 4) */
+    uint32_t max_reads;        /* largest request accepted (default 131072) */
+    uint32_t max_read_len;     /* default 300 */
+    uint32_t max_win_len;      /* default max_read_len + 128 */
+    uint64_t mem_budget_bytes; /* device scratch admitted at once (default 16 GiB) */
+} esp_server_config;
+
+typedef struct esp_server esp_server;
+
+int esp_server_create(esp_genome *g, const esp_extend_params *params,
+                      const esp_server_config *cfg, int device, esp_server **out);
+/* Non-blocking.  ESP_EBUSY: the request alone exceeds the memory budget or
+ * max_reads; ESP_ECLOSED: the server is closing. */
+int esp_server_submit(esp_server *s, const esp_serve_request *req, uint64_t *ticket);
+/* Wait (bounded) for a ticket: ESP_OK with *status the request's status and
+ * *latency_ms submit-to-results time, or ESP_ETIMEOUT. */
+int esp_server_wait(esp_server *s, uint64_t ticket, int timeout_ms, int32_t *status,
+                    double *latency_ms);
+/* Stop admitting: pending (not yet admitted) requests complete with
+ * ESP_ECLOSED; in-flight ones finish normally. */
+int esp_server_close(esp_server *s);
+int esp_server_destroy(esp_server *s);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----
  *
  * esp_batch_run_band_noalloc: the same banded/full-matrix DP with traceback
@@ -419,6 +474,17 @@ int esp_synth_splice(uint64_t seed, uint64_t n_reads, uint8_t *genome_arena,
                      uint64_t genome_bytes, esp_contig *contigs, uint8_t *read_arena,
                      uint64_t read_bytes, esp_splice_read *reads, esp_splice_cand *cands,
                      uint64_t n_cands);
+
+/* Serve workload (config 4): a uniform-ACGT genome of `total_bases` in
+ * `n_contigs` equal contigs (contig c starts at base c * stride, stride a
+ * multiple of 4), and request reads: 2x150 paired-end fragments (insert
+ * 250-450) at uniform coordinates with the Gotoh error model; each read's
+ * window is read +- 32 with hint offset 32. */
+int esp_synth_genome(uint64_t seed, uint64_t total_bases, uint32_t n_contigs, uint8_t *arena,
+                     uint64_t arena_bytes, esp_contig *contigs);
+int esp_synth_serve_reads(uint64_t seed, uint64_t request, const uint8_t *genome_arena,
+                          const esp_contig *contigs, uint32_t n_contigs, uint64_t n_reads,
+                          uint8_t *read_arena, uint64_t read_arena_bytes, esp_serve_read *reads);
 
 /* Number of device kernel launches the last batch call enqueued. */
 uint64_t esp_last_launch_count(const esp_handle *h);

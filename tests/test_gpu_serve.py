@@ -1,0 +1,85 @@
+"""The serving loop: results are identical alone and in a concurrent mix,
+match the batch API and the oracle, and admission / closing behave."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import oracle as O  # noqa: E402
+from esperanto_gb300 import EspError  # noqa: E402
+from esperanto_gb300 import batch as B  # noqa: E402
+from esperanto_gb300 import serve as SV  # noqa: E402
+from esperanto_gb300.split import Genome  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def setup():
+    garena, contigs = SV.synth_genome(5, 4_000_000, 4)
+    g = Genome(garena, contigs)
+    srv = SV.Server(g, n_streams=3, max_reads=32768, mem_budget=2 << 30)
+    yield garena, contigs, g, srv
+    srv.destroy()
+
+
+def _key(t, k):
+    o = t.out[k]
+    return (int(o["score"]), int(o["read_start"]), int(o["read_end"]), int(o["ref_start"]),
+            tuple(B.cigar_of(t.cigar.reshape(len(t.reads), t.stride)[k], int(o["n_ops"]))))
+
+
+def test_alone_equals_mix_equals_batch_and_oracle(setup):
+    garena, contigs, g, srv = setup
+    arena, reads = SV.synth_request(5, 1, garena, contigs, 3000)
+    alone = srv.submit(arena, reads)
+    st, lat = srv.wait(alone)
+    assert st == 0 and lat > 0
+    ref = [_key(alone, k) for k in range(len(reads))]
+    # the same request in a mix of concurrent requests of other sizes
+    mix = []
+    for k, n in enumerate([800, 20000, 3000, 12000, 500, 30000, 7000, 1000]):
+        a2, r2 = SV.synth_request(5, 100 + k, garena, contigs, n)
+        mix.append(srv.submit(a2, r2))
+        if k == 3:
+            again = srv.submit(arena, reads)
+    for t in mix + [again]:
+        assert srv.wait(t)[0] == 0
+    assert [_key(again, k) for k in range(len(reads))] == ref
+    # the batch API on the same pairs (windows read from a genome copy)
+    pairs = SV.serve_pairs(reads, contigs)
+    read_bits = B.unpack_codes(arena, 0, len(reads) * 150)
+    gb = B.unpack_codes(garena, 0, int(contigs["base"][-1] + contigs["len"][-1]))
+    codes = np.concatenate([read_bits, gb])
+    comb = B.pack_codes(codes)
+    pairs2 = pairs.copy()
+    pairs2["win_pos"] = pairs["win_pos"] + len(reads) * 150
+    out, cig = B.extend_batch_host(pairs2, comb, mode=B.MODE_HINT, cigar_stride=32)
+    for k in range(len(reads)):
+        o = out[k]
+        assert (int(o["score"]), int(o["read_start"]), int(o["read_end"]), int(o["ref_start"]),
+                tuple(B.cigar_of(cig[k], int(o["n_ops"])))) == ref[k]
+    # the oracle on a sample
+    for k in range(0, len(reads), 97):
+        r = B._ASCII[read_bits[k * 150:(k + 1) * 150]].tobytes()
+        ws, wl = int(pairs["win_pos"][k]), int(pairs["win_len"][k])
+        w = B._ASCII[gb[ws:ws + wl]].tobytes()
+        assert O.extend_hint(r, w, O.Params(), offset=int(pairs["band_offset"][k])).key() == ref[k]
+
+
+def test_admission_and_close(setup):
+    garena, contigs, g, srv = setup
+    arena, reads = SV.synth_request(5, 7, garena, contigs, 40000)  # > max_reads
+    with pytest.raises(EspError):
+        srv.submit(arena, reads)
+    srv2 = SV.Server(g, n_streams=1, max_reads=32768, mem_budget=1 << 30)
+    ts = [srv2.submit(*SV.synth_request(5, 200 + k, garena, contigs, 20000)) for k in range(6)]
+    srv2.close()
+    sts = [srv2.wait(t)[0] for t in ts]
+    assert sts[0] == 0                      # already admitted: finishes normally
+    assert any(s == -8 for s in sts[1:])    # still queued at close: ESP_ECLOSED
+    with pytest.raises(EspError):
+        srv2.submit(*SV.synth_request(5, 300, garena, contigs, 100))
+    srv2.destroy()
