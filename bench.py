@@ -389,6 +389,19 @@ def dist_init(args):
     return rank, world, local
 
 
+def reduce_over_ranks(ms, cells, e2e_s, e2e_cells, world, device="cpu"):
+    """Whole-job figures of a weak-scaling run: the slowest rank's time and
+    the units all ranks processed (kernel-timed and end-to-end legs)."""
+    import torch
+    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=device)
+    c = torch.tensor([float(cells), float(e2e_cells)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(c[0]), float(t[1]), float(c[1])
+
+
 def reference_arm(args, wl, seed, threads, n_pairs):
     run, sample = wl.cpu_reference(seed, args.cpu_sample, threads)
     for _ in range(args.warmup):
@@ -471,25 +484,23 @@ def main():
             wl.step()
             evs[k + 1].record(stream)
     torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     clocks = clk.stop(local)
     per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     ms = sum(per_step) / args.steps
     launches = int(L.esp_last_launch_count(buf.handle)) * args.steps
-    tmax = torch.tensor([ms], dtype=torch.float64, device=dev)
-    tcells = torch.tensor([float(wl.cells)], dtype=torch.float64, device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tcells, op=dist.ReduceOp.SUM)
-    ms_max = float(tmax.item())
-    value = float(tcells.item()) / (ms_max / 1e3) / 1e9
 
     wl.e2e_step()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         wl.e2e_step()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    e2e_val = wl.cells / e2e_s / 1e9
+    ms_max, cells_all, e2e_max, e2e_cells_all = reduce_over_ranks(ms, wl.cells, e2e_s, wl.cells,
+                                                                  world, dev)
+    value = cells_all / (ms_max / 1e3) / 1e9
+    e2e_val = e2e_cells_all / e2e_max / 1e9
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

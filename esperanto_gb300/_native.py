@@ -134,6 +134,7 @@ def lib():
                                              C.POINTER(ExtensionC), vp, C.c_uint32]
     L.esp_run_band.argtypes = ext_args + [C.c_int64, C.c_int64, C.POINTER(ExtensionC), vp,
                                           C.c_uint32]
+    L.esp_score_tail_win.argtypes = ext_args + [C.POINTER(ExtensionC), vp, C.c_uint32]
     L.esp_batch_extend_host.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
                                         C.c_uint64, C.POINTER(ExtendParamsC), vp, vp, C.c_uint32]
     L.esp_batch_extend_device.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,

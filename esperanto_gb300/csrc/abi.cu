@@ -274,6 +274,14 @@ int esp_extend_hint(esp_handle *h, const uint8_t *read, size_t read_len,
                     30, out, cigar, cigar_cap);
 }
 
+int esp_score_tail_win(esp_handle *h, const uint8_t *tail, size_t tail_len,
+                       const uint8_t *ref_window, size_t window_len,
+                       const esp_extend_params *params, esp_extension *out, uint32_t *cigar,
+                       uint32_t cigar_cap) {
+    return one_pair(h, ESP_MODE_HINT, tail, tail_len, ref_window, window_len, params, 0, 30, out,
+                    cigar, cigar_cap);
+}
+
 int esp_run_band(esp_handle *h, const uint8_t *read, size_t read_len, const uint8_t *ref_window,
                  size_t window_len, const esp_extend_params *params, int64_t band_offset,
                  int64_t band_half, esp_extension *out, uint32_t *cigar, uint32_t cigar_cap) {

@@ -6,6 +6,7 @@ the GB300 kernels, plus the resident genome it reads windows from.
 * ``retry_tail_start``  -- split.rs:150-223 (same arguments and result).
 * ``channel_a_batch``   -- channel A (split.rs:468-570) over many reads, each
                            with its library candidates, + build_rescue_ext.
+* ``score_tail_win``    -- splice.rs:667-684; ``tail_gate`` splice.rs:705-708.
 Every DP runs on the GPU; there is no CPU path.
 """
 from __future__ import annotations
@@ -136,6 +137,27 @@ class Genome:
             self.close()
         except Exception:
             pass
+
+
+def score_tail_win(tail, ref_window, params: ExtendParams = ExtendParams(),
+                   buf: Optional[ExtendBuffer] = None) -> Extension:
+    """splice.rs:667-684: extend_hint of a tail along the direct diagonal."""
+    buf = buf or _default_buffer()
+    tail, ref_window = _b(tail), _b(ref_window)
+    p = params._c()
+    cap = 2 * (len(tail) + len(ref_window)) + 8
+    ops = (C.c_uint32 * cap)()
+    out = N.ExtensionC()
+    buf.check(N.lib().esp_score_tail_win(buf.handle, tail, len(tail), ref_window,
+                                         len(ref_window), C.byref(p), C.byref(out), ops, cap))
+    return Extension(out.read_start, out.read_end, out.ref_start, decode_cigar(ops[:out.n_ops]),
+                     out.score)
+
+
+def tail_gate(ext: Extension, tail_len: int) -> bool:
+    """splice.rs:705-708: aligned >= 4/5 of the tail and a positive score."""
+    aligned = max(ext.read_end - ext.read_start, 0)
+    return aligned * 5 >= tail_len * 4 and ext.score > 0
 
 
 def retry_tail_start(genome: Genome, read, tail_start: int, j: Junction, signal: int,

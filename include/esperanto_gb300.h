@@ -107,6 +107,14 @@ int esp_extend_hint(esp_handle *h, const uint8_t *read, size_t read_len,
                     uint32_t hint_den, esp_extension *out, uint32_t *cigar,
                     uint32_t cigar_cap);
 
+/* score_tail_win (crates/map/src/splice.rs:667-684): a tail scored against
+ * its reference window by extend_hint along the direct diagonal (offset 0,
+ * slope 1/1).  Same outputs and errors as esp_extend_hint. */
+int esp_score_tail_win(esp_handle *h, const uint8_t *tail, size_t tail_len,
+                       const uint8_t *ref_window, size_t window_len,
+                       const esp_extend_params *params, esp_extension *out, uint32_t *cigar,
+                       uint32_t cigar_cap);
+
 /* run_band (extend.rs:606-851) with an explicit band, exposed for kernel
  * equivalence checks the way the reference's own tests call it.  half < 0
  * selects the full matrix (band_spec None). */

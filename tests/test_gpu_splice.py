@@ -114,3 +114,28 @@ def test_config3_subset_channel_a():
                B.cigar_of(cig[r], int(o["n_ops"])))
         assert got == (want.cand, want.dro, want.pos, want.score, want.signal, want.cigar), r
     assert n_found > len(reads) // 2
+
+
+def test_score_tail_win_vs_oracle():
+    """splice.rs:667-684: score_tail_win is extend_hint at offset 0; tail_gate
+    (splice.rs:705-708) on its result."""
+    rng = random.Random(0x7A11)
+    n = 0
+    for _ in range(300):
+        tl = rng.randint(0, 60)
+        tail = "".join(rng.choice("ACGTN" if rng.random() < 0.1 else "ACGT") for _ in range(tl))
+        wl = tl + rng.randint(0, 40)
+        win = list("".join(rng.choice("ACGT") for _ in range(wl)))
+        k = rng.randint(0, max(0, wl - tl))
+        for q in range(min(tl, wl - k)):  # plant the tail with a few edits
+            if rng.random() > 0.05:
+                win[k + q] = tail[q] if tail[q] != "N" else "A"
+        win = "".join(win)
+        d = rng.choice([0, 1, 2])
+        got = S.score_tail_win(tail, win, S.ExtendParams(edit_dir=d))
+        want = O.extend_hint(tail, win, O.Params(edit_dir=d), offset=0)
+        assert got.key() == want.key(), (tail, win, d)
+        gate = want.read_end - want.read_start
+        assert S.tail_gate(got, tl) == (gate * 5 >= tl * 4 and want.score > 0)
+        n += 1
+    assert n == 300
