@@ -189,6 +189,7 @@ static int one_pair(esp_handle *h, int mode, const uint8_t *read, size_t m, cons
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
+    if (m > (size_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     CK(h, cudaSetDevice(h->device));
     std::vector<esp_n_interval> iv;
     uint64_t wpos = ((m + 63) / 64) * 64;  // window starts on a 16-byte boundary
@@ -316,6 +317,7 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     CK(h, cudaSetDevice(h->device));
     Limits L1, L2;
     batch_common(h, mode, pairs, n_pairs, L1, L2);
+    if (L1.max_m > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     size_t sz_pairs = (n_pairs * sizeof(esp_pair) + 255) / 256 * 256;
     size_t sz_iv = (n_iv_count * sizeof(esp_n_interval) + 255) / 256 * 256;
     size_t sz_arena = (arena_bytes + 16 + 255) / 256 * 256;
@@ -360,6 +362,7 @@ int esp_batch_extend_device(esp_handle *h, int mode, const esp_pair *pairs, uint
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
+    if (limits->max_read_len > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     CK(h, cudaSetDevice(h->device));
     Limits L1, L2;
     if (mode == ESP_MODE_HINT) {

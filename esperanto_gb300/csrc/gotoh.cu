@@ -639,7 +639,7 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     const uint64_t wbases = job.win_arena ? job.win_arena_bases : job.arena_bases;
     if ((uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
         P.read_pos + (uint64_t)m > job.arena_bases || P.win_pos + (uint64_t)n > wbases ||
-        m > 32767 || n > 32767) {
+        m > 32767 || n > 32767 || m > K.max_m) {
         o.status = ESP_EINVAL;  // pair outside the arena / N table: refuse
         job.out[pi] = o;
         return;
@@ -719,6 +719,11 @@ int make_gotoh_const(const esp_extend_params &p, GotohConst &k) {
     if (p.edit_dir == ESP_EDIT_AG) lut[10] = 0;  // read G / ref A
     if (p.edit_dir == ESP_EDIT_TC) lut[8] = 0;   // read C / ref T
     for (int i = 0; i < 25; i++) k.lut[i] = (int8_t)lut[i];
+    // The row buffer keeps 4E (signed) and 4H + 2 in 16 bits, so every H and
+    // E must stay <= 8191; H <= m * (largest substitution score).
+    int smax = 0;
+    for (int i = 0; i < 25; i++) smax = lut[i] > smax ? lut[i] : smax;
+    k.max_m = smax > 0 ? 8191 / smax : 32767;
     for (int rc = 0; rc < 5; rc++) {
         uint32_t w[2] = {0, 0};
         for (int fc = 0; fc < 8; fc++) {

@@ -100,16 +100,86 @@ __device__ __forceinline__ void add_chain<8>(uint32_t (&s)[8], const uint32_t (&
 
 constexpr int MY_BLOCK = 128;
 
+// 16 text codes of one window in processing order: the code of the first
+// column in bits 31:30, its N flag in bit 31 of `n`.
+struct CodeWin {
+    uint32_t c, n;
+};
+
+// Split 16 packed 2-bit codes (code k at bits 31-2k, 30-2k) into a high-bit
+// and a low-bit mask with position k at bit k.
+__device__ __forceinline__ void unshuffle16(uint32_t cw, uint32_t &hi, uint32_t &lo) {
+    uint32_t x = __brev(cw);  // code k -> bits 2k (high), 2k+1 (low)
+    uint32_t e = x & 0x55555555u, o = (x >> 1) & 0x55555555u;
+    e = (e | (e >> 1)) & 0x33333333u;
+    e = (e | (e >> 2)) & 0x0f0f0f0fu;
+    e = (e | (e >> 4)) & 0x00ff00ffu;
+    e = (e | (e >> 8)) & 0x0000ffffu;
+    o = (o | (o >> 1)) & 0x33333333u;
+    o = (o | (o >> 2)) & 0x0f0f0f0fu;
+    o = (o | (o >> 4)) & 0x00ff00ffu;
+    o = (o | (o >> 8)) & 0x0000ffffu;
+    hi = e;
+    lo = o;
+}
+
+// Pattern rows of 32 read positions starting at position `b` (may be
+// negative: positions < 0 are absent): high/low code bits and the mask of
+// real ACGT positions (bit k <-> position b + k).
+__device__ __forceinline__ void read_limb(const MyersJob &job, const esp_myers_pair &P,
+                                          const esp_n_interval *iv, int m, int b, uint32_t &hi,
+                                          uint32_t &lo, uint32_t &real) {
+    hi = lo = real = 0;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        int s = b + 16 * half;  // first position of this 16-position half
+        if (s + 16 <= 0 || s >= m) continue;
+        int start = s < 0 ? 0 : s;
+        int skip = start - s;  // leading absent positions (s < 0)
+        uint32_t cw = load16(job.arena, P.read_pos + (uint64_t)start);
+        uint32_t nm = P.n_read ? nmask16(iv, P.n_read, start) : 0u;
+        uint32_t h, l;
+        unshuffle16(cw, h, l);
+        uint32_t nb = __brev(nm) & 0xffffu;  // position start + k -> bit k
+        int cnt = min(16 - skip, m - start);
+        uint32_t v = (cnt >= 16 ? 0xffffu : ((1u << cnt) - 1u)) & ~nb;  // read N matches nothing
+        int sh = 16 * half + skip;
+        hi |= h << sh;
+        lo |= l << sh;
+        real |= v << sh;
+    }
+}
+
+// EA Peq rows for text A, C, G, T from one limb's code bits.
+__device__ __forceinline__ void ea_rows(uint32_t hi, uint32_t lo, uint32_t real,
+                                        uint32_t (&rows)[4]) {
+    uint32_t a = ~hi & ~lo & real, c = ~hi & lo & real, g = hi & ~lo & real,
+             tt = hi & lo & real;
+    rows[0] = a | g;   // text A: read A or G
+    rows[1] = c;       // text C: read C
+    rows[2] = g;       // text G: read G
+    rows[3] = tt | c;  // text T: read T or C
+}
+
 // One pair.  flags: MYF_REVERSE (best start: read and text both reversed,
 // myers_ea.rs:158-185), MYF_GLOBAL (engine global: leading column +1 per text
 // base, engine/src/myers.rs:151-169).
-template <int NW>
+//
+// TOP (every non-global search): the m pattern rows occupy the TOP m bits of
+// the NW*32-bit vector, so the last row is always bit 31 of limb NW-1 and the
+// score update needs no runtime limb select.  The bits below are virtual
+// rows that match every text base and start with vertical delta 0: they keep
+// D = 0 in every column (their horizontal deltas are 0, they never carry into
+// the real rows and they shift 0 into real row 0), which is the semi-global
+// boundary the real rows had with hin = 0.  Global search (hin = +1) keeps
+// the pattern in the low bits.
+template <int NW, bool TOP>
 __device__ void myers_pair(const MyersJob &job, uint32_t k, uint32_t *__restrict__ peq) {
     const esp_myers_pair P = job.pairs[k];
     const int m = (int)P.read_len;
     const int64_t n = P.text_len;
     const bool rev = job.flags & MYF_REVERSE;
-    const bool glob = job.flags & MYF_GLOBAL;
+    const bool glob = !TOP;
     esp_myers_result res;
     res.dist = m;
     res.pos = 0;
@@ -121,133 +191,124 @@ __device__ void myers_pair(const MyersJob &job, uint32_t k, uint32_t *__restrict
     }
     const esp_n_interval *iv = job.n_iv + P.n_first;
     const uint32_t bs = blockDim.x, t = threadIdx.x;
-    // Peq rows: text code 0..3, row 4 (text N) all zero.  Each 32-position
-    // limb is built in registers: the 2-bit codes are split into a high-bit
-    // and a low-bit mask (position k -> bit k) and combined per EA rule.
-#pragma unroll
-    for (int w = 0; w < NW; w++) {
-        uint32_t hi = 0, lo = 0, valid = 0;
-        int base = w * 32;
-        if (base < m) {
-            int cnt = min(32, m - base);
-            valid = cnt >= 32 ? 0xffffffffu : ((1u << cnt) - 1u);
-            uint32_t nmask = 0;
-#pragma unroll
-            for (int half = 0; half < 2; half++) {
-                int b16 = base + 16 * half;
-                if (b16 >= m) break;
-                uint32_t cw = load16(job.arena, P.read_pos + (uint64_t)b16);
-                // code k at bits (31-2k, 30-2k): reverse so code k sits at
-                // bits (2k = high, 2k+1 = low), then unshuffle even/odd bits
-                uint32_t x = __brev(cw);
-                uint32_t e = x & 0x55555555u, o = (x >> 1) & 0x55555555u;
-                e = (e | (e >> 1)) & 0x33333333u;
-                e = (e | (e >> 2)) & 0x0f0f0f0fu;
-                e = (e | (e >> 4)) & 0x00ff00ffu;
-                e = (e | (e >> 8)) & 0x0000ffffu;
-                o = (o | (o >> 1)) & 0x33333333u;
-                o = (o | (o >> 2)) & 0x0f0f0f0fu;
-                o = (o | (o >> 4)) & 0x00ff00ffu;
-                o = (o | (o >> 8)) & 0x0000ffffu;
-                hi |= e << (16 * half);
-                lo |= o << (16 * half);
-                if (P.n_read) nmask |= __brev(nmask16(iv, P.n_read, b16)) << (16 * half);
-            }
-            valid &= ~nmask;  // read N matches nothing
-        }
-        uint32_t a = ~hi & ~lo & valid, c = ~hi & lo & valid, g = hi & ~lo & valid,
-                 tt = hi & lo & valid;
-        uint32_t rows[4] = {a | g, c, g, tt | c};  // text A, C, G, T
-        if (!rev) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) peq[(q * NW + w) * bs + t] = rows[q];
-            peq[(4 * NW + w) * bs + t] = 0u;
-        } else {
-            // reversed read: position i -> bit m-1-i; stored after all limbs
-#pragma unroll
-            for (int q = 0; q < 4; q++) peq[(q * NW + w) * bs + t] = rows[q];
-        }
-    }
-    if (rev) {
-        // Reverse each row as one m-bit vector (position i -> bit m-1-i):
-        // bit-reverse over this pair's own nwp limbs (nwp*32 - m < 32 padding
-        // bits), then shift the padding out.  Sources are re-read from shared
-        // memory, where a runtime limb index costs nothing.
-        const int nwp = (m + 31) >> 5;
-        const int pad = nwp * 32 - m;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            uint32_t dst[NW];
-#pragma unroll
-            for (int w = 0; w < NW; w++) {
-                uint32_t r0 = 0, r1 = 0;
-                if (w < nwp) {
-                    r0 = __brev(peq[(q * NW + (nwp - 1 - w)) * bs + t]);
-                    if (w + 1 < nwp) r1 = __brev(peq[(q * NW + (nwp - 2 - w)) * bs + t]);
-                }
-                dst[w] = pad ? __funnelshift_r(r0, r1, pad) : r0;
-            }
-#pragma unroll
-            for (int w = 0; w < NW; w++) peq[(q * NW + w) * bs + t] = dst[w];
-        }
-#pragma unroll
-        for (int w = 0; w < NW; w++) peq[(4 * NW + w) * bs + t] = 0u;
-    }
+    const int off = TOP ? NW * 32 - m : 0;  // virtual rows below the pattern
     uint32_t pv[NW], mv[NW];
+    // Peq rows: text code 0..3, row 4 (text N): virtual rows only.
+    if (!rev) {
+        // forward: limb w bit k <-> read position w*32 + k - off
 #pragma unroll
-    for (int w = 0; w < NW; w++) {
-        int lo = w * 32;
-        pv[w] = m >= lo + 32 ? 0xffffffffu : (m > lo ? ((1u << (m - lo)) - 1u) : 0u);
-        mv[w] = 0u;
+        for (int w = 0; w < NW; w++) {
+            uint32_t hi, lo, real;
+            read_limb(job, P, iv, m, w * 32 - off, hi, lo, real);
+            uint32_t rows[4];
+            ea_rows(hi, lo, real, rows);
+            const int vb = off - w * 32;  // virtual bits of this limb: [0, vb)
+            const uint32_t virt = !TOP || vb <= 0 ? 0u : (vb >= 32 ? 0xffffffffu : (1u << vb) - 1u);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                peq[(q * NW + w) * bs + t] = rows[q] | virt;
+                peq[((4 + q) * NW + w) * bs + t] = virt;  // text N: virtual rows only
+            }
+            // pattern rows start with vertical delta +1 (D[i][0] = i)
+            if (TOP) {
+                pv[w] = ~virt;
+            } else {
+                const int lim = m - w * 32;
+                pv[w] = lim >= 32 ? 0xffffffffu : (lim > 0 ? (1u << lim) - 1u : 0u);
+            }
+            mv[w] = 0u;
+        }
+    } else {
+        // reversed (TOP only): bottom-aligned forward limbs F (position p at
+        // bit p) reversed as one NW*32-bit vector: position p -> bit
+        // NW*32 - 1 - p, i.e. R[w] = brev(F[NW-1-w]); the padding above m
+        // lands in the virtual bits [0, off).
+        uint32_t F[4][NW];
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            uint32_t hi, lo, real;
+            read_limb(job, P, iv, m, w * 32, hi, lo, real);
+            uint32_t rows[4];
+            ea_rows(hi, lo, real, rows);
+#pragma unroll
+            for (int q = 0; q < 4; q++) F[q][w] = rows[q];
+        }
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            const int vb = off - w * 32;
+            const uint32_t virt = vb <= 0 ? 0u : (vb >= 32 ? 0xffffffffu : (1u << vb) - 1u);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                peq[(q * NW + w) * bs + t] = __brev(F[q][NW - 1 - w]) | virt;
+                peq[((4 + q) * NW + w) * bs + t] = virt;
+            }
+            pv[w] = ~virt;
+            mv[w] = 0u;
+        }
     }
-    const int topw = (m - 1) >> 5;
+    const int topw = (m - 1) >> 5;  // global layout only
     const uint32_t topb = 1u << ((m - 1) & 31);
     int score = m, best = m;
-    int64_t best_at = 0;
+    uint32_t best_at = 0, col = 0;
     const uint32_t hin = glob ? 1u : 0u;
     const esp_n_interval *tiv = iv + P.n_read;
     for (int64_t base = 0; base < n; base += 16) {
         int cnt = (int)min((int64_t)16, n - base);
-        // text position of column index x: forward x, reversed n-1-x
-        int64_t q0 = rev ? (n - base - 16) : base;  // first position of the 16-base window
-        uint32_t cw, nm;
-        if (rev && q0 < 0) {
-            // short leading window of a reversed scan: fetch [0, 16) and shift
-            cw = load16(job.arena, P.text_pos);
-            nm = P.n_text ? nmask16(tiv, P.n_text, 0) : 0u;
-            int sh = (int)(-q0);
-            cw >>= 2 * sh;
-            nm >>= sh;
-            q0 = 0;
+        CodeWin win;
+        if (!rev) {
+            win.c = load16(job.arena, P.text_pos + (uint64_t)base);
+            win.n = P.n_text ? nmask16(tiv, P.n_text, base) : 0u;
         } else {
-            cw = load16(job.arena, P.text_pos + (uint64_t)q0);
-            nm = P.n_text ? nmask16(tiv, P.n_text, q0) : 0u;
+            // right-aligned window [n-base-16, n-base): slot 15 first
+            int64_t q0 = n - base - 16;
+            uint32_t cw, nm;
+            if (q0 < 0) {
+                cw = load16(job.arena, P.text_pos);
+                nm = P.n_text ? nmask16(tiv, P.n_text, 0) : 0u;
+                int sh = (int)(-q0);
+                cw >>= 2 * sh;
+                nm >>= sh;
+            } else {
+                cw = load16(job.arena, P.text_pos + (uint64_t)q0);
+                nm = P.n_text ? nmask16(tiv, P.n_text, q0) : 0u;
+            }
+            uint32_t x = __brev(cw);  // slot s -> bits 2s (high), 2s+1 (low)
+            win.c = ((x >> 1) & 0x55555555u) | ((x & 0x55555555u) << 1);
+            win.n = __brev(nm) << 16;
         }
 #pragma unroll 4
         for (int x = 0; x < cnt; x++) {
-            // forward: position base+x is slot x of the window; reversed:
-            // position n-1-(base+x) is slot 15-x of the (right-aligned) window
-            int slot = rev ? (15 - x) : x;
-            uint32_t c = (cw >> (30 - 2 * slot)) & 3u;
-            if ((nm >> (31 - slot)) & 1u) c = 4u;
-            uint32_t eq[NW], xv[NW], s[NW], ph[NW], mh[NW];
+            uint32_t c = (win.c >> 30) | ((win.n >> 29) & 4u);  // text N: rows 4..7
+            win.c <<= 2;
+            win.n <<= 1;
+            const uint32_t *pe = peq + (c * NW) * bs + t;
+            uint32_t xv[NW], s[NW], ph[NW], mh[NW];
 #pragma unroll
             for (int w = 0; w < NW; w++) {
-                eq[w] = peq[(c * NW + w) * bs + t];
-                xv[w] = eq[w] | mv[w];
-                s[w] = eq[w] & pv[w];
+                uint32_t eq = pe[w * bs];
+                xv[w] = eq | mv[w];
+                s[w] = eq & pv[w];
             }
             add_chain<NW>(s, s, pv);
-            uint32_t hp = 0, hm = 0;
 #pragma unroll
             for (int w = 0; w < NW; w++) {
                 uint32_t xh = (s[w] ^ pv[w]) | xv[w];
                 ph[w] = mv[w] | ~(xh | pv[w]);
                 mh[w] = pv[w] & xh;
-                if (w == topw) {
-                    hp = ph[w] & topb;
-                    hm = mh[w] & topb;
+            }
+            int d;
+            if (TOP) {
+                d = (int)(ph[NW - 1] >> 31) - (int)(mh[NW - 1] >> 31);
+            } else {
+                uint32_t hp = 0, hm = 0;
+#pragma unroll
+                for (int w = 0; w < NW; w++) {
+                    if (w == topw) {
+                        hp = ph[w] & topb;
+                        hm = mh[w] & topb;
+                    }
                 }
+                d = (hp ? 1 : 0) - (hm ? 1 : 0);
             }
 #pragma unroll
             for (int w = NW - 1; w >= 0; w--) {
@@ -256,10 +317,11 @@ __device__ void myers_pair(const MyersJob &job, uint32_t k, uint32_t *__restrict
                 pv[w] = mhs | ~(xv[w] | phs);
                 mv[w] = phs & xv[w];
             }
-            score += (hp ? 1 : 0) - (hm ? 1 : 0);
-            if (!glob && score < best) {
+            score += d;
+            col++;
+            if (TOP && score < best) {
                 best = score;
-                best_at = base + x + 1;
+                best_at = col;
             }
         }
     }
@@ -273,23 +335,29 @@ __device__ void myers_pair(const MyersJob &job, uint32_t k, uint32_t *__restrict
     job.out[k] = res;
 }
 
-template <int NW>
+template <int NW, bool TOP>
 __global__ void __launch_bounds__(MY_BLOCK) myers_kernel(MyersJob job) {
     extern __shared__ uint32_t smem[];
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < job.n_pairs;
          k += (uint64_t)gridDim.x * blockDim.x)
-        myers_pair<NW>(job, (uint32_t)k, smem);
+        myers_pair<NW, TOP>(job, (uint32_t)k, smem);
 }
 
 cudaError_t launch_myers(const MyersJob &job, int nw, int num_sms, cudaStream_t st) {
     if (job.n_pairs == 0) return cudaSuccess;
-    size_t smem = (size_t)5 * nw * MY_BLOCK * sizeof(uint32_t);
+    size_t smem = (size_t)8 * nw * MY_BLOCK * sizeof(uint32_t);
+
     uint64_t need = (job.n_pairs + MY_BLOCK - 1) / MY_BLOCK;
     uint64_t cap = (uint64_t)num_sms * 16;
     int grid = (int)(need < cap ? need : cap);
     switch (nw) {
-#define ESP_MY_CASE(W) \
-    case W: myers_kernel<W><<<grid, MY_BLOCK, smem, st>>>(job); break;
+#define ESP_MY_CASE(W)                                                   \
+    case W:                                                              \
+        if (job.flags & MYF_GLOBAL)                                      \
+            myers_kernel<W, false><<<grid, MY_BLOCK, smem, st>>>(job);   \
+        else                                                             \
+            myers_kernel<W, true><<<grid, MY_BLOCK, smem, st>>>(job);    \
+        break;
         ESP_MY_CASE(1) ESP_MY_CASE(2) ESP_MY_CASE(3) ESP_MY_CASE(4)
         ESP_MY_CASE(5) ESP_MY_CASE(6) ESP_MY_CASE(7) ESP_MY_CASE(8)
 #undef ESP_MY_CASE

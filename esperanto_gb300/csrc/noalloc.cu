@@ -73,6 +73,7 @@ extern "C" int esp_batch_run_band_noalloc(const esp_pair *pairs, uint64_t n_pair
     if (n_pairs > 0xffffffffull - 64) return ESP_EINVAL;
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK) return ESP_EDOMAIN;
+    if (limits->max_read_len > (uint32_t)K.max_m) return ESP_EDOMAIN;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ESP_ECUDA;
     int rc = setup_device(dev);

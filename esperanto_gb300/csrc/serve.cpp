@@ -238,7 +238,8 @@ int esp_server_create(esp_genome *g, const esp_extend_params *params,
     if (!c.max_read_len) c.max_read_len = 300;
     if (!c.max_win_len) c.max_win_len = c.max_read_len + 128;
     if (!c.mem_budget_bytes) c.mem_budget_bytes = 16ull << 30;
-    if (c.max_read_len > 32767 || c.max_win_len > 32767) {
+    if (c.max_read_len > 32767 || c.max_win_len > 32767 ||
+        c.max_read_len > (uint32_t)s->K.max_m) {
         delete s;
         return ESP_EDOMAIN;
     }

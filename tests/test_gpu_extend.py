@@ -161,3 +161,19 @@ def test_cigar_capacity_reported():
         rc = N.lib().esp_extend(buf.handle, read, len(read), win, len(win), C.byref(p),
                                 C.byref(out), ops, 1)
         buf.check(rc)
+
+
+def test_score_range_domain():
+    """The row buffer holds H and E in int16 lanes: reads up to 8191 / (largest
+    substitution score) bases run (4095 at the default +2 match) and match the
+    oracle; one base more is refused with ESP_EDOMAIN instead of wrapping."""
+    rng = np.random.default_rng(77)
+    read = "".join(rng.choice(list("ACGT"), 4095))
+    win = "AC" + read[:2000] + "G" + read[2000:] + "TT"
+    got, _ = E.run_band(read, win, band=(2, 40))
+    want, _ = O.run_dispatch(read, win, band=(2, 40))
+    assert got.score == want.score and got.key() == want.key()
+    assert got.score > 8000
+    with pytest.raises(E.EspError) as ei:
+        E.run_band(read + "A", win + "A", band=(2, 40))
+    assert ei.value.code == -4  # ESP_EDOMAIN

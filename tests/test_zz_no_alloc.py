@@ -109,7 +109,7 @@ def test_noalloc_matches_regular_entry_point_twice():
 
 def test_noalloc_rejects_work_beyond_its_scratch():
     L = _lib()
-    lim = N.BatchLimitsC(30000, 30000, -1)  # full matrices far larger than the array
+    lim = N.BatchLimitsC(4000, 30000, -1)  # full matrices far larger than the array
     p = ExtendParams()._c()
     dummy = torch.zeros(64, dtype=torch.uint8, device="cuda")
     rc = L.esp_batch_run_band_noalloc(dummy.data_ptr(), 1, dummy.data_ptr(), 64, None, 0,
