@@ -74,6 +74,14 @@ class SpliceParamsC(C.Structure):
                 ("known_bonus", C.c_int32), ("refine_radius", C.c_uint32)]
 
 
+class PaidxInfoC(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("w", C.c_uint32), ("freq_cutoff", C.c_uint32),
+                ("contig_count", C.c_uint32), ("kmer_count", C.c_uint64),
+                ("positions_count", C.c_uint64), ("fasta_sha256", C.c_uint8 * 32),
+                ("arena_bytes", C.c_uint64), ("n_iv_count", C.c_uint64),
+                ("names_bytes", C.c_uint64)]
+
+
 class RetryOutcomeC(C.Structure):
     _fields_ = [("found", C.c_int32), ("dro", C.c_uint32), ("left_win_lo", C.c_uint32),
                 ("total", C.c_int32), ("left", ExtensionC), ("right", ExtensionC)]
@@ -157,6 +165,10 @@ def lib():
     L.esp_genome_create.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint32, vp, C.c_uint64,
                                     C.POINTER(vp)]
     L.esp_genome_destroy.argtypes = [vp]
+    L.esp_paidx_scan.argtypes = [vp, C.c_uint64, C.POINTER(PaidxInfoC), C.c_char_p, sz]
+    L.esp_paidx_contigs.argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint32, vp,
+                                    C.c_uint64, vp, C.c_uint64]
+    L.esp_genome_from_paidx.argtypes = [vp, vp, C.c_uint64, C.POINTER(vp)]
     L.esp_retry_tail_start.argtypes = [vp, vp, u8p, sz, C.c_uint32, C.POINTER(JunctionC), C.c_int,
                                        C.c_uint32, C.POINTER(SpliceParamsC),
                                        C.POINTER(ExtendParamsC), C.POINTER(RetryOutcomeC), vp, vp,

@@ -7,6 +7,9 @@ the GB300 kernels, plus the resident genome it reads windows from.
 * ``channel_a_batch``   -- channel A (split.rs:468-570) over many reads, each
                            with its library candidates, + build_rescue_ext.
 * ``score_tail_win``    -- splice.rs:667-684; ``tail_gate`` splice.rs:705-708.
+* ``paidx_contigs``     -- the contigs of a paidx v1 index (index_io.rs),
+                           validated as the reference's loader does;
+                           ``Genome.from_paidx`` makes them resident.
 Every DP runs on the GPU; there is no CPU path.
 """
 from __future__ import annotations
@@ -123,6 +126,12 @@ class Genome:
             iv["start"], iv["end"] = n_iv[:, 0], n_iv[:, 1]
         return cls(B.pack_codes(allc), contigs, iv, buf)
 
+    @classmethod
+    def from_paidx(cls, data, buf: Optional[ExtendBuffer] = None) -> "Genome":
+        """The contigs of a paidx v1 index (bytes or a path), resident."""
+        arena, contigs, iv, _names, _info = paidx_contigs(data)
+        return cls(arena, contigs, iv, buf)
+
     @property
     def handle(self):
         return self._g
@@ -137,6 +146,53 @@ class Genome:
             self.close()
         except Exception:
             pass
+
+
+class PaidxError(ValueError):
+    """A malformed (ESP_EFORMAT) or unsupported (ESP_EVERSION) paidx file;
+    the message is the reference loader's."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+def _paidx_bytes(data) -> bytes:
+    if isinstance(data, (bytes, bytearray, memoryview)):
+        return bytes(data)
+    with open(data, "rb") as f:
+        return f.read()
+
+
+def paidx_scan(data) -> "N.PaidxInfoC":
+    """Validate a paidx v1 file (index_io.rs:237-354 decode_parts) and size
+    its contents; raises PaidxError with the reference's message."""
+    raw = _paidx_bytes(data)
+    info = N.PaidxInfoC()
+    msg = C.create_string_buffer(256)
+    rc = N.lib().esp_paidx_scan(raw, len(raw), C.byref(info), msg, 256)
+    if rc != 0:
+        raise PaidxError(rc, msg.value.decode())
+    return info
+
+
+def paidx_contigs(data):
+    """(arena, contigs, n_intervals, names, info) of a paidx v1 file, laid
+    out as a resident genome (each contig byte-aligned in the arena)."""
+    raw = _paidx_bytes(data)
+    info = paidx_scan(raw)
+    arena = np.zeros(max(1, info.arena_bytes), np.uint8)
+    contigs = np.zeros(info.contig_count, CONTIG_DTYPE)
+    iv = np.zeros(max(1, info.n_iv_count), B.NIV_DTYPE)
+    names = C.create_string_buffer(max(1, info.names_bytes))
+    rc = N.lib().esp_paidx_contigs(raw, len(raw), arena.ctypes.data, len(arena),
+                                   contigs.ctypes.data if len(contigs) else None, len(contigs),
+                                   iv.ctypes.data, len(iv), names, len(names))
+    if rc != 0:
+        raise PaidxError(rc, "esp_paidx_contigs failed")
+    nm = names.raw[:info.names_bytes].split(b"\0")[:info.contig_count]
+    return (arena[:info.arena_bytes], contigs, iv[:info.n_iv_count],
+            [x.decode("utf-8", "replace") for x in nm], info)
 
 
 def score_tail_win(tail, ref_window, params: ExtendParams = ExtendParams(),

@@ -40,6 +40,8 @@ extern "C" {
 #define ESP_ETIMEOUT (-7) /* bounded wait expired                            */
 #define ESP_ECLOSED (-8)  /* queue closed                                    */
 #define ESP_ESCRATCH (-9) /* work too large for the fixed no-allocation scratch */
+#define ESP_EFORMAT (-10) /* malformed index file (AlignError::IndexFormat)  */
+#define ESP_EVERSION (-11) /* unsupported index version (AlignError::IndexVersion) */
 
 #define ESP_OP_M 0
 #define ESP_OP_I 1
@@ -263,6 +265,35 @@ int esp_genome_create(esp_handle *h, const uint8_t *arena, uint64_t arena_bytes,
                       const esp_contig *contigs, uint32_t n_contigs,
                       const esp_n_interval *n_iv, uint64_t n_iv_count, esp_genome **out);
 int esp_genome_destroy(esp_genome *g);
+
+/* ---- paidx v1 index contigs: crates/map/src/index_io.rs ----
+ *
+ * The reference's index loader (index_io.rs:113-121 load, :237-354
+ * decode_parts) validates the whole file and keeps its Reference: the
+ * contigs, already 2-bit packed MSB-first with their N intervals.  These
+ * entry points run the same strict validation (same failure messages) and
+ * lay the contigs out as a resident genome, each contig starting on a byte
+ * of the arena.  The seeding tables are validated, not kept. */
+typedef struct {
+    uint32_t k, w, freq_cutoff, contig_count;
+    uint64_t kmer_count, positions_count;
+    uint8_t fasta_sha256[32];
+    uint64_t arena_bytes;  /* bytes of packed contigs (the genome arena) */
+    uint64_t n_iv_count;   /* N intervals over all contigs */
+    uint64_t names_bytes;  /* contig names, each NUL-terminated */
+} esp_paidx_info;
+
+/* Validate `data` (the whole file) and size its contents.  ESP_EFORMAT /
+ * ESP_EVERSION with the reference's message in `msg` when it is malformed. */
+int esp_paidx_scan(const uint8_t *data, uint64_t len, esp_paidx_info *info, char *msg,
+                   size_t msg_cap);
+/* Copy the contigs into caller buffers sized by esp_paidx_scan (host only). */
+int esp_paidx_contigs(const uint8_t *data, uint64_t len, uint8_t *arena, uint64_t arena_bytes,
+                      esp_contig *contigs, uint32_t n_contigs, esp_n_interval *n_iv,
+                      uint64_t n_iv_count, char *names, uint64_t names_bytes);
+/* Validate and upload: a resident genome whose contig c is the index's
+ * contig c (the reference's Reference of a loaded Index). */
+int esp_genome_from_paidx(esp_handle *h, const uint8_t *data, uint64_t len, esp_genome **out);
 
 /* ---- splice-rescue flank DP: crates/map/src/split.rs ---- */
 

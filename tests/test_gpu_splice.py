@@ -139,3 +139,31 @@ def test_score_tail_win_vs_oracle():
         assert S.tail_gate(got, tl) == (gate * 5 >= tl * 4 and want.score > 0)
         n += 1
     assert n == 300
+
+
+def test_genome_from_paidx_matches_sequences():
+    """A genome loaded from a paidx v1 index (contigs byte-aligned in the
+    arena) gives the same retries as one built from the sequences."""
+    from paidx_writer import encode
+    rng = random.Random(0xDA1D)
+    contigs = [_rand_contig(rng, n, 3) for n in (1203, 5001, 777)]
+    raw = encode([(f"c{k}", s) for k, s in enumerate(contigs)])
+    g1 = S.Genome.from_paidx(raw)
+    g2 = S.Genome.from_sequences(contigs)
+    n = 0
+    for _ in range(60):
+        c = rng.randrange(len(contigs))
+        seq = contigs[c]
+        start = rng.randrange(200, len(seq) - 300)
+        end = start + rng.randrange(60, 250)
+        b = rng.randrange(20, 130)
+        read = seq[start - b:start] + seq[end:end + 150 - b]
+        j = S.Junction(c, start, end, rng.random() < 0.3)
+        a1 = S.retry_tail_start(g1, read, b, j, S.SIG_GTAG, 3)
+        a2 = S.retry_tail_start(g2, read, b, j, S.SIG_GTAG, 3)
+        assert (a1 is None) == (a2 is None)
+        if a1 is not None:
+            assert (a1.dro, a1.left_win_lo, a1.total, a1.left.key(), a1.right.key()) == \
+                (a2.dro, a2.left_win_lo, a2.total, a2.left.key(), a2.right.key())
+            n += 1
+    assert n > 10
