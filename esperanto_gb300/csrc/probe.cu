@@ -1,0 +1,80 @@
+// probe.cu -- measured integer issue peaks of this GPU, the denominators of
+// the DP kernels' roofline (the measured peaks cover HBM and bf16
+// only).  Each probe thread runs 8 independent dependency chains of one
+// instruction kind, long enough that issue, not latency, is the limit; the
+// result is lane-operations per second.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "esp_host.h"
+
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kIters = 4096;
+
+template <int KIND>
+__global__ void __launch_bounds__(256) int_probe(uint32_t seed, uint32_t *sink) {
+    uint32_t x[kChains];
+    const uint32_t y = seed * 0x9E3779B9u + threadIdx.x, z = seed ^ 0x7F4A7C15u;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) x[c] = threadIdx.x * (c + 1) + blockIdx.x;
+#pragma unroll 1
+    for (int it = 0; it < kIters; it++) {
+#pragma unroll
+        for (int c = 0; c < kChains; c++) {
+            if (KIND == 0) {  // 3-input logic
+                asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(x[c]) : "r"(y), "r"(z));
+            } else if (KIND == 1) {  // integer max
+                asm volatile("max.s32 %0, %0, %1;" : "+r"(x[c]) : "r"(y + c));
+            } else if (KIND == 2) {  // integer add
+                asm volatile("add.u32 %0, %0, %1;" : "+r"(x[c]) : "r"(y));
+            } else {  // integer multiply-add
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y | 1u), "r"(z));
+            }
+        }
+    }
+    uint32_t acc = 0;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) acc ^= x[c];
+    if (acc == seed) sink[0] = acc;  // keeps the chains live
+}
+
+template <int KIND>
+int run(int sms, cudaStream_t st, uint32_t *sink, double *out) {
+    const int blocks = sms * 8, threads = 256;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    int_probe<KIND><<<blocks, threads, 0, st>>>(1u, sink);  // warm-up
+    cudaEventRecord(a, st);
+    const int reps = 5;
+    for (int r = 0; r < reps; r++) int_probe<KIND><<<blocks, threads, 0, st>>>(r + 2u, sink);
+    cudaEventRecord(b, st);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess || ms <= 0) return ESP_ECUDA;
+    double ops = (double)reps * blocks * threads * kChains * kIters;
+    *out = ops / (ms * 1e-3);
+    return ESP_OK;
+}
+
+}  // namespace
+
+extern "C" int esp_int_peaks(esp_handle *h, double *lop3, double *imnmx, double *iadd,
+                             double *imad) {
+    if (!h || !lop3 || !imnmx || !iadd || !imad) return ESP_EINVAL;
+    CK(h, cudaSetDevice(h->device));
+    uint32_t *sink = nullptr;
+    CK(h, cudaMalloc((void **)&sink, 4));
+    int rc = run<0>(h->num_sms, h->stream, sink, lop3);
+    if (rc == ESP_OK) rc = run<1>(h->num_sms, h->stream, sink, imnmx);
+    if (rc == ESP_OK) rc = run<2>(h->num_sms, h->stream, sink, iadd);
+    if (rc == ESP_OK) rc = run<3>(h->num_sms, h->stream, sink, imad);
+    cudaFree(sink);
+    return rc == ESP_OK ? ESP_OK : fail(h, rc, "integer peak probe failed");
+}

@@ -451,6 +451,12 @@ int esp_server_wait(esp_server *s, uint64_t ticket, int timeout_ms, int32_t *sta
 int esp_server_close(esp_server *s);
 int esp_server_destroy(esp_server *s);
 
+/* ---- measured integer issue peaks (no counterpart in the reference) ----
+ * Lane-operations per second of dependent-free streams of 3-input logic,
+ * integer max, integer add and integer multiply-add on the handle's GPU: the
+ * denominators of the DP kernels' integer roofline.  Runs a few milliseconds of probes. */
+int esp_int_peaks(esp_handle *h, double *lop3, double *imnmx, double *iadd, double *imad);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----
  *
  * esp_batch_run_band_noalloc: the same banded/full-matrix DP with traceback

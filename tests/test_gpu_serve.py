@@ -75,7 +75,10 @@ def test_admission_and_close(setup):
     with pytest.raises(EspError):
         srv.submit(arena, reads)
     srv2 = SV.Server(g, n_streams=1, max_reads=32768, mem_budget=1 << 30)
-    ts = [srv2.submit(*SV.synth_request(5, 200 + k, garena, contigs, 20000)) for k in range(6)]
+    # requests are built first so that all six are queued within microseconds
+    # and the single slot is still busy with the first when close() lands
+    reqs = [SV.synth_request(5, 200 + k, garena, contigs, 30000) for k in range(6)]
+    ts = [srv2.submit(*r) for r in reqs]
     srv2.close()
     sts = [srv2.wait(t)[0] for t in ts]
     assert sts[0] == 0                      # already admitted: finishes normally
