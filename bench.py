@@ -34,15 +34,35 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Integer ops per cell of the DP recurrence as written in csrc/gotoh.cu
-# (E 3, F 3, key clears 3, LUT select 1, diag add 1, H max 3, H tag 1,
-# traceback bits 4, row-max key 2).
-OPS_PER_CELL = 21
-# Myers: 10 32-bit ops per 32-cell limb per text column (wide-word step).
+# Integer-ALU-pipe ops per cell of the DP recurrence as written in
+# csrc/gotoh.cu (E 3, F 3, tag clears 2, LUT select + diag add + floor 3,
+# H key 3, H tag 1, traceback-bit selects 2, row max 1); the three
+# multiply-adds per cell (traceback accumulators, row-max key) issue on the
+# FMA pipe and are not counted.
+OPS_PER_CELL = 18
+# Myers: 10 32-bit logic/add/shift ops per 32-cell limb per text column.
 MYERS_OPS_PER_CELL = 10.0 / 32.0
-INT_LANES_PER_SM = 128
+# ncu DRAM bytes (read + write) of the DP kernel per launch, from the
+# committed summaries: config 0 (65,536 pairs, one launch) and config 1
+# (1,048,576 Myers pairs, one launch); config 2 per DP cell, captured on a
+# 524,288-pair case of the same distribution and scaled by cells.
+TRAFFIC_BYTES = {0: 50.3e6 + 348.3e6, 1: 125.5e6 + 9.3e6}
+TRAFFIC_PER_CELL = {2: (2713001472 + 6431804160) / 7716062109}
+TRAFFIC_SOURCE = {0: "profiles/gotoh_kernel_config0_65536pairs.md",
+                  1: "profiles/myers_kernel_config1_1048576pairs.md",
+                  2: "profiles/gotoh_kernel_traffic_config2.md (scaled by cells)"}
 DEFAULT_PAIRS = {0: 65536, 1: 1048576, 2: 4194304, 3: 524288}
 SEEDS = {0: 1, 1: 2, 2: 3, 3: 4}
+
+
+def int_peak(L, buf):
+    """Measured integer-ALU issue peak of this GPU (lane-ops/s): the slower
+    of the 3-input-logic and integer-max probe streams (esp_int_peaks)."""
+    v = [C.c_double() for _ in range(4)]
+    buf.check(L.esp_int_peaks(buf.handle, *[C.byref(x) for x in v]))
+    lop3, imnmx, iadd, imad = (x.value for x in v)
+    return min(lop3, imnmx), {"lop3": lop3 / 1e12, "imnmx": imnmx / 1e12,
+                              "iadd": iadd / 1e12, "imad": imad / 1e12}
 
 
 def load_peaks():
@@ -171,6 +191,39 @@ class GotohWorkload(Workload):
         self.h2d = pin_arena.nbytes + pin_pairs.nbytes
         self.d2h = out_pin.nbytes + cig_pin.nbytes
         self.input_mb = arena.nbytes / 1e6
+
+    def plain_per_call(self, seed, sample, buf):
+        """The plain per-call drop-in (esp_run_band, host buffers, one pair per
+        call, as the reference's callers invoke run_band/extend) on a sample
+        of the same workload: pairs/s."""
+        from esperanto_gb300 import _native as N
+        from esperanto_gb300 import batch as B
+        from esperanto_gb300.extend import ExtendParams
+        L = N.lib()
+        arena, pairs = B.synth_gotoh(seed, sample, self.config)
+        cases = []
+        for k in range(sample):
+            r = B._ASCII[B.unpack_codes(arena, int(pairs["read_pos"][k]),
+                                        int(pairs["read_len"][k]))].tobytes()
+            w = B._ASCII[B.unpack_codes(arena, int(pairs["win_pos"][k]),
+                                        int(pairs["win_len"][k]))].tobytes()
+            cases.append((r, w, int(pairs["band_offset"][k]), int(pairs["band_half"][k])))
+        p = ExtendParams()._c()
+        out = N.ExtensionC()
+        cap = 4096
+        ops = (C.c_uint32 * cap)()
+        fn = L.esp_run_band
+
+        def one(c):
+            buf.check(fn(buf.handle, c[0], len(c[0]), c[1], len(c[1]), C.byref(p), c[2], c[3],
+                         C.byref(out), ops, cap))
+        for c in cases[:16]:
+            one(c)
+        t = time.perf_counter()
+        for c in cases:
+            one(c)
+        dt = time.perf_counter() - t
+        return sample / dt, f"{sample} pairs of the same workload, one esp_run_band call each"
 
     def cpu_reference(self, seed, sample, threads):
         import oracle as O
@@ -508,10 +561,19 @@ def main():
         return
 
     peaks, src = load_peaks()
-    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    max_mhz = peaks.get("sm_max_mhz", 2070.0)
-    peak_ops = sm_count * INT_LANES_PER_SM * max_mhz * 1e6 / 1e12
-    achieved_ops = wl.cells * wl.ops_per_cell / (ms / 1e3) / 1e12
+    peak_ops, probe = int_peak(L, buf)
+    achieved_ops = wl.cells * wl.ops_per_cell / (ms / 1e3)
+    traffic = None
+    if config in TRAFFIC_BYTES and n_pairs == DEFAULT_PAIRS[config]:
+        traffic = TRAFFIC_BYTES[config]
+    elif config in TRAFFIC_PER_CELL:
+        traffic = TRAFFIC_PER_CELL[config] * wl.cells
+    plain = None
+    if hasattr(wl, "plain_per_call"):
+        pps, sample = wl.plain_per_call(seed, 2000, buf)
+        batched_pps = n_pairs / (ms / 1e3)
+        plain = {"pairs_per_s": pps, "sample": sample,
+                 "batched_pairs_per_s": batched_pps, "batched_over_plain": batched_pps / pps}
     cpu = None
     if not args.no_cpu_baseline:
         run, sample = wl.cpu_reference(seed, args.cpu_sample, threads)
@@ -532,11 +594,15 @@ def main():
         "pairs_per_s": n_pairs * world / (ms_max / 1e3),
         "bad_status": bad,
         "gpu_launches": launches,
-        "roofline": {"bound": "int_alu", "achieved": achieved_ops, "peak": peak_ops,
-                     "unit": "Tops/s", "frac": achieved_ops / peak_ops, "traffic": None,
-                     "peak_source": f"nominal: {sm_count} SMs x {INT_LANES_PER_SM} INT32 lanes "
-                                    f"x {max_mhz:.0f} MHz ({src} max clock)",
-                     "ops_per_cell": wl.ops_per_cell},
+        "roofline": {"bound": "int_alu", "achieved": achieved_ops / 1e12,
+                     "peak": peak_ops / 1e12, "unit": "Tops/s",
+                     "frac": achieved_ops / peak_ops, "traffic": traffic,
+                     "traffic_source": TRAFFIC_SOURCE.get(config),
+                     "peak_source": "measured on this GPU (esp_int_peaks: independent streams "
+                                    "of 3-input logic / integer max, the ALU-pipe issue rate)",
+                     "probe_tops": probe, "ops_per_cell": wl.ops_per_cell,
+                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": src},
+        "plain_per_call": plain,
         "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(wl.h2d),
                 "d2h_bytes_per_step": int(wl.d2h)},
         "cpu_baseline": cpu,
