@@ -26,6 +26,56 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     if (n_pairs == 0) return ESP_OK;
     if (n_pairs > 0xffffffffull - 64) return fail(h, ESP_EINVAL, "batch too large");
     int rc;
+    if (h->warp_max < 0) {
+        const char *v = getenv("ESP_WARP_MAX");
+        h->warp_max = v ? atol(v) : 8192;
+    }
+    if (n_pairs <= (uint64_t)h->warp_max) {
+        // Few pairs: one warp per pair (the wavefront kernel), so a lone
+        // pair is not latency-bound on a single thread.
+        uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
+        uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
+        uint64_t per_warp_bytes = (tbw + rbw) * 4;
+        uint64_t warps = std::min<uint64_t>(n_pairs, (uint64_t)h->num_sms * 12);
+        warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes));
+        warps = (warps + 3) / 4 * 4;  // whole blocks: every launched warp owns its scratch
+        if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * per_warp_bytes)) != ESP_OK)
+            return rc;
+        if (mode == ESP_MODE_HINT &&
+            (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
+            return rc;
+        CK(h, cudaMemsetAsync(h->d_ctr, 0, 64, st));
+        esp::GotohJob job{};
+        job.pairs = d_pairs;
+        job.n_pairs = n_pairs;
+        job.arena = d_arena;
+        job.arena_bases = arena_bytes * 4;
+        job.win_arena = d_win_arena;
+        job.win_arena_bases = win_arena_bytes * 4;
+        job.n_iv = d_iv;
+        job.n_iv_count = n_iv;
+        job.out = d_out;
+        job.cigar = d_cigar;
+        job.cigar_stride = cigar_stride;
+        job.tb = h->d_tb;
+        job.tb_words = tbw;
+        job.rb_words = rbw;
+        job.esc_list = h->d_esc;
+        job.esc_count = h->d_ctr + 4;
+        job.mode = mode == ESP_MODE_HINT ? 1 : 0;
+        job.max_m = (int)L1.max_m;
+        CK(h, esp::launch_gotoh_warp(job, K, (int)warps, st));
+        h->launches++;
+        if (mode == ESP_MODE_HINT) {
+            esp::GotohJob j2 = job;
+            j2.mode = 2;
+            j2.list = h->d_esc;
+            j2.list_count = h->d_ctr + 4;
+            CK(h, esp::launch_gotoh_warp(j2, K, (int)warps, st));
+            h->launches++;
+        }
+        return ESP_OK;
+    }
     // scratch slots: one warp per 32 pairs up to the resident limit, bounded
     // by the scratch budget
     uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
@@ -143,6 +193,12 @@ int esp_create(esp_handle **out, int device) {
         return ESP_ECUDA;
     }
     *out = h;
+    return ESP_OK;
+}
+
+int esp_set_warp_max(esp_handle *h, long warp_max) {
+    if (!h || warp_max < 0) return ESP_EINVAL;
+    h->warp_max = warp_max;
     return ESP_OK;
 }
 

@@ -21,6 +21,7 @@ struct esp_handle {
     uint64_t launches = 0;
     int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
     int variant = -1;   // DP kernel variant; -1 = ESP_GOTOH_VARIANT env or default
+    long warp_max = -1; // batches of at most this many pairs run warp-per-pair; -1 = ESP_WARP_MAX or 8192
     uint64_t scratch_budget = 8ull << 30;  // bytes of DP scratch one launch may use
     // grow-only device buffers
     void *d_in = nullptr;       // per-call staging: pair | n intervals | arena

@@ -62,6 +62,12 @@ cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, in
                          cudaStream_t st, int variant);
 constexpr int kGotohVariants = 2;
 
+// Warp-per-pair DP kernel (per-call drop-in, small batches): `warps` warps
+// stride over the pairs; each warp owns tb_words + rb_words words of the
+// traceback scratch (job.tb), job.rb unused.  Same results as launch_gotoh.
+cudaError_t launch_gotoh_warp(const GotohJob &job, const GotohConst &k, int warps,
+                              cudaStream_t st);
+
 // Resident blocks per SM of the DP kernel at `block` threads.
 int gotoh_blocks_per_sm(int block, int variant);
 

@@ -306,6 +306,7 @@ __device__ __forceinline__ int kind_op(int k) { return k < 3 ? ESP_OP_M : (k < 5
 // window, or on an H START cell.  Word loads are cached and the word of the
 // next column is prefetched (most steps move one column left in the strip);
 // read and window codes are cached 16 bases at a time.
+template <int TBS>
 struct Walker {
     const Geo &g;
     const uint32_t *tb;
@@ -361,13 +362,13 @@ struct Walker {
         } else if (idx == nk) {
             w = nw;
         } else {
-            w = tb[(size_t)idx * 32];
+            w = tb[(size_t)idx * TBS];
         }
         ck = idx;
         cw = w;
         if (j - 1 >= cclo) {  // prefetch the word one column left (same strip)
             nk = idx - 1;
-            nw = tb[(size_t)nk * 32];
+            nw = tb[(size_t)nk * TBS];
         } else {
             nk = -1;
         }
@@ -420,6 +421,9 @@ struct CigarOut {
 };
 
 // Traceback, end trimming, rebuild and neutral flanks (extend.rs:864-1068).
+// TBS: word stride of the traceback (32 for the lane-interleaved scratch of
+// the thread-per-pair kernel, 1 for the warp-per-pair kernel's own scratch).
+template <int TBS>
 __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, const Geo &g,
                           const uint32_t *tb, int sw, int m, int n, const Seq &read,
                           const Seq &win, const FillResult &F, esp_extension &o, uint32_t *cig,
@@ -429,7 +433,7 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
     // walk 1: number of steps N, total T, trail; steps recorded for walk 2
     int N = 0, P = 0, trail = 0;
     {
-        Walker W(g, tb, sw, read, win, K, F.best_i, F.best_j);
+        Walker<TBS> W(g, tb, sw, read, win, K, F.best_i, F.best_j);
         int kind;
         uint32_t acc = 0;
         while (W.step(kind)) {
@@ -465,7 +469,7 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
         // middle step) is captured on the way in case that happens.
         bool degenerate = (T <= 0);  // u = -1
         const int tstar = N - 1 - N / 2;
-        Walker W(g, tb, sw, read, win, K, F.best_i, F.best_j);
+        Walker<TBS> W(g, tb, sw, read, win, K, F.best_i, F.best_j);
         int i = F.best_i, j = F.best_j;
         int pos_acc = 0;
         bool found = false;
@@ -605,13 +609,27 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
     o.score = score;
 }
 
-__device__ void process_pair(const GotohJob &job, const GotohConst &K,
-                             const uint32_t *__restrict__ s_lut, const int8_t *__restrict__ lut,
-                             uint32_t pi, uint32_t *tb, uint32_t *rb) {
-    if (pi >= job.n_pairs) return;  // corrupt work list: never index past the batch
+// A validated pair: geometry for the job's mode, sequences, output slot and
+// the result record being built.
+struct PairSetup {
+    int m, n, sw;
+    bool full;
+    Geo g;
+    Seq read, win;
+    uint32_t *cig;
+    esp_extension o;
+};
+
+// Validate pair pi and resolve its band geometry (extend.rs:392-428 for the
+// extend_hint attempts).  Returns true when a DP is needed; otherwise the
+// result (empty extension, or a refusal) has been written when `write`.
+__device__ __forceinline__ bool setup_pair(const GotohJob &job, const GotohConst &K, uint32_t pi,
+                                           uint64_t tb_cap, uint64_t rb_cap, bool write,
+                                           PairSetup &S) {
+    if (pi >= job.n_pairs) return false;  // corrupt work list: never index past the batch
     esp_pair P = job.pairs[pi];
     int m = (int)P.read_len, n = (int)P.win_len;
-    esp_extension o;
+    esp_extension &o = S.o;
     o.read_start = o.read_end = o.ref_start = 0;
     o.score = 0;
     o.n_ops = 0;
@@ -619,15 +637,18 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     o.touched = o.touch_left = o.touch_clamped = 0;
     o.escalated = job.mode == 2 ? 1 : 0;
     o.status = ESP_OK;
-    uint32_t *cig = job.cigar + (uint64_t)pi * job.cigar_stride;
+    S.cig = job.cigar + (uint64_t)pi * job.cigar_stride;
     if (m == 0 || n == 0) {  // extend.rs:430-442 empty_extension
         if (m > 0) {
             o.n_ops = 1;
-            if (job.cigar_stride >= 1) cig[0] = ((uint32_t)m << 4) | ESP_OP_S;
-            else o.status = ESP_ECAP;
+            if (job.cigar_stride >= 1) {
+                if (write) S.cig[0] = ((uint32_t)m << 4) | ESP_OP_S;
+            } else {
+                o.status = ESP_ECAP;
+            }
         }
-        job.out[pi] = o;
-        return;
+        if (write) job.out[pi] = o;
+        return false;
     }
     Geo g;
     bool full;
@@ -648,35 +669,48 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
     int sw = full ? n : min(2 * g.half + STRIP, n);
     uint64_t need_tb = (uint64_t)((m + STRIP - 1) / STRIP) * (uint64_t)sw;
     uint64_t need_rb = (uint64_t)sw;
-    if (need_tb > job.tb_words || need_rb > job.rb_words) {
-        o.status = ESP_EINVAL;  // scratch sized too small by the host: refuse, never overrun
-        job.out[pi] = o;
-        return;
-    }
     const uint8_t *warena = job.win_arena ? job.win_arena : job.arena;
     const uint64_t wbases = job.win_arena ? job.win_arena_bases : job.arena_bases;
-    if ((uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
+    if (need_tb > tb_cap || need_rb > rb_cap ||
+        (uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
         P.read_pos + (uint64_t)m > job.arena_bases || P.win_pos + (uint64_t)n > wbases ||
         m > 32767 || n > 32767 || m > K.max_m) {
-        o.status = ESP_EINVAL;  // pair outside the arena / N table: refuse
-        job.out[pi] = o;
-        return;
+        // scratch sized too small by the host, or the pair lies outside its
+        // tables: refuse, never overrun
+        o.status = ESP_EINVAL;
+        if (write) job.out[pi] = o;
+        return false;
     }
     const esp_n_interval *iv = job.n_iv + P.n_first;
-    Seq read{job.arena, P.read_pos, iv, P.n_read};
-    Seq win{warena, P.win_pos, iv + P.n_read, P.n_win};
-    FillResult F = win.cnt ? dp_fill<true>(K, s_lut, m, n, g, read, win, tb, sw, rb)
-                           : dp_fill<false>(K, s_lut, m, n, g, read, win, tb, sw, rb);
-    dp_finish(K, lut, g, tb, sw, m, n, read, win, F, o, cig, job.cigar_stride);
+    S.read = Seq{job.arena, P.read_pos, iv, P.n_read};
+    S.win = Seq{warena, P.win_pos, iv + P.n_read, P.n_win};
+    S.m = m;
+    S.n = n;
+    S.sw = sw;
+    S.full = full;
+    S.g = g;
+    return true;
+}
+
+// Traceback, CIGAR, TouchRec, extend_hint escalation (extend.rs:421-426),
+// then the result record.
+template <int TBS>
+__device__ __forceinline__ void finish_pair(const GotohJob &job, const GotohConst &K,
+                                            const int8_t *__restrict__ lut, uint32_t pi,
+                                            PairSetup &S, const FillResult &F,
+                                            const uint32_t *tb) {
+    esp_extension &o = S.o;
+    dp_finish<TBS>(K, lut, S.g, tb, S.sw, S.m, S.n, S.read, S.win, F, o, S.cig,
+                   job.cigar_stride);
     if (F.trow) {
         o.touched = 1;
         o.touch_row = F.trow;
         o.touch_left = F.tleft ? 1 : 0;
         o.touch_clamped = F.tclamp ? 1 : 0;
     }
-    if (job.mode == 1 && !full) {
-        // extend.rs:421-426: escalate on a band-edge touch or < 85% of perfect
-        int perfect = m * K.match;
+    if (job.mode == 1 && !S.full) {
+        // escalate on a band-edge touch or < 85% of perfect
+        int perfect = S.m * K.match;
         if (F.trow != 0 || o.score * 20 < perfect * 17) {
             uint32_t slot = atomicAdd(job.esc_count, 1u);
             job.esc_list[slot] = pi;
@@ -684,6 +718,16 @@ __device__ void process_pair(const GotohJob &job, const GotohConst &K,
         }
     }
     job.out[pi] = o;
+}
+
+__device__ void process_pair(const GotohJob &job, const GotohConst &K,
+                             const uint32_t *__restrict__ s_lut, const int8_t *__restrict__ lut,
+                             uint32_t pi, uint32_t *tb, uint32_t *rb) {
+    PairSetup S;
+    if (!setup_pair(job, K, pi, job.tb_words, job.rb_words, true, S)) return;
+    FillResult F = S.win.cnt ? dp_fill<true>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, rb)
+                             : dp_fill<false>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, rb);
+    finish_pair<32>(job, K, lut, pi, S, F, tb);
 }
 
 template <int MINB>
@@ -713,6 +757,173 @@ __global__ void __launch_bounds__(128, MINB) gotoh_kernel(GotohJob job, GotohCon
             process_pair(job, K, s_lut, s_lut25, pi, tb, rb);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-per-pair DP (the per-call drop-in and small batches).  One pair's
+// strips are spread over the lanes of a warp (lane s owns rows 8s+1..8s+8 of
+// the current 32-strip pass) and swept as a wavefront: at step t lane s
+// evaluates column j = t - s, receiving the bottom row (H, E) of lane s-1 at
+// the same column by a warp shuffle (lane s-1 produced it one step earlier)
+// and keeping the previous step's value as its diagonal.  Idle or
+// out-of-window lanes publish H = 0, E = NEG -- what the thread-per-pair
+// kernel's row buffer presents outside the previous strip's window -- so
+// every cell, traceback word, row maximum and touch is the same as there.
+// A pass of 32 strips hands its last row to the next pass through the row
+// buffer.  Lane 0 then walks the traceback.  Scratch is the warp's own
+// (word stride 1).
+// ---------------------------------------------------------------------------
+
+__device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict__ s_lut,
+                                const PairSetup &P, uint32_t *tb, uint32_t *rb, int lane) {
+    const int m = P.m, n = P.n, sw = P.sw;
+    const Geo &g = P.g;
+    const uint32_t ABSENT = __byte_perm(2u, (uint32_t)NEG4, 0x5410);  // H = 0, E = NEG
+    FillResult R;
+    R.bestHp = 2;
+    R.best_i = R.best_j = 0;
+    R.trow = 0;
+    R.tleft = R.tclamp = false;
+    const int nstrips = (m + STRIP - 1) / STRIP;
+    for (int base = 0; base < nstrips; base += 32) {
+        const int s = base + lane;
+        const bool act = s < nstrips;
+        const int i0 = s * STRIP + 1;
+        const int nact = act ? min(STRIP, m - i0 + 1) : 0;
+        Strip S;
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            S.lo[r] = g.lo(i0 + r);
+            S.hi[r] = g.hi(i0 + r);
+            S.Hl[r] = 2;
+            S.Fl[r] = NEG4;
+            S.rk[r] = -1;
+            S.hr[r] = -1;
+        }
+        const int clo = S.lo[0];
+        const int chi = act ? g.hi(i0 + nact - 1) : 0;
+        const int lo7 = S.lo[STRIP - 1];
+        if (act) {
+            uint32_t rw = load16(P.read.arena, P.read.pos + (uint64_t)(i0 - 1));
+            uint32_t rn = P.read.cnt ? nmask16(P.read.iv, P.read.cnt, i0 - 1) : 0u;
+#pragma unroll
+            for (int r = 0; r < STRIP; r++) {
+                uint32_t c = (rw >> (30 - 2 * r)) & 3u;
+                if ((rn >> (31 - r)) & 1u) c = 4;
+                S.l0[r] = s_lut[2 * c];
+                S.l1[r] = s_lut[2 * c + 1];
+            }
+        }
+        // the previous pass's last strip left its bottom row in rb, columns
+        // [plo, phi] of row 8*base
+        const int plo = base ? g.lo(base * STRIP) : 0, phi = base ? g.hi(base * STRIP) : -1;
+        int t0 = act ? clo + lane : 0x7fffffff, t1 = act ? chi + lane : -1;
+        t0 = __reduce_min_sync(0xffffffffu, t0);
+        t1 = __reduce_max_sync(0xffffffffu, t1);
+        uint32_t pub = ABSENT;  // bottom row published at the end of a step
+        int diag = 2;           // H of the row above at the previous column
+        if (lane == 0 && base && clo - 1 >= plo && clo - 1 <= phi)
+            diag = (int)(rb[clo - 1 - plo] & 0xffffu);
+        uint32_t *tbs = tb + (size_t)s * sw;
+        const bool handoff = lane == 31 && s + 1 < nstrips;
+        for (int t = t0; t <= t1; t++) {
+            uint32_t in = __shfl_up_sync(0xffffffffu, pub, 1);
+            const int j = t - lane;
+            if (lane == 0) in = (base && j >= plo && j <= phi) ? rb[j - plo] : ABSENT;
+            uint32_t out = ABSENT;
+            if (act && j >= clo && j <= chi) {
+                uint32_t code = P.win.cnt ? P.win.code(j - 1)
+                                          : load1(P.win.arena, P.win.pos + (uint64_t)(j - 1));
+                uint32_t sel = code * 0x1111u + 0x8880u;
+                int upH = (int)(in & 0xffffu), upE = ((int)in) >> 16;
+                uint32_t word = dp_column<1>(S, K, j, sel, 32767u - (uint32_t)j, upH, upE, diag);
+                tbs[j - clo] = word;
+                out = __byte_perm((uint32_t)upH, (uint32_t)upE, 0x5410);
+                if (handoff && j >= lo7) rb[j - lo7] = out;
+            }
+            diag = (int)(in & 0xffffu);
+            pub = out;
+        }
+        __syncwarp();
+        // this lane's rows, in row order (extend.rs:795-827)
+        int bHp = -1, bi = 0, bj = 0, trow = 0;
+        bool tleft = false, tclamp = false;
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            if (r < nact) {
+                int rowHp = S.rk[r] >> 15;
+                int argj = 32767 - (S.rk[r] & 32767);
+                if (trow == 0) {
+                    if (argj == S.lo[r]) {
+                        trow = i0 + r;
+                        tleft = true;
+                        tclamp = S.lo[r] <= 1;
+                    } else if (S.hi[r] < n && S.hr[r] == rowHp) {
+                        trow = i0 + r;
+                        tleft = false;
+                        tclamp = S.hi[r] >= n;
+                    }
+                }
+                if (rowHp > bHp) {
+                    bHp = rowHp;
+                    bi = i0 + r;
+                    bj = argj;
+                }
+            }
+        }
+        // merge lanes in row order: the first strictly larger maximum wins,
+        // the first touching row wins
+        const int mx = __reduce_max_sync(0xffffffffu, bHp);
+        const int wl = __ffs(__ballot_sync(0xffffffffu, bHp == mx)) - 1;
+        const int wi = __shfl_sync(0xffffffffu, bi, wl), wj = __shfl_sync(0xffffffffu, bj, wl);
+        if (mx > R.bestHp) {
+            R.bestHp = mx;
+            R.best_i = wi;
+            R.best_j = wj;
+        }
+        const uint32_t tm = __ballot_sync(0xffffffffu, trow != 0);
+        if (R.trow == 0 && tm) {
+            const int tl = __ffs(tm) - 1;
+            R.trow = __shfl_sync(0xffffffffu, trow, tl);
+            R.tleft = __shfl_sync(0xffffffffu, (int)tleft, tl) != 0;
+            R.tclamp = __shfl_sync(0xffffffffu, (int)tclamp, tl) != 0;
+        }
+    }
+    return R;
+}
+
+__global__ void __launch_bounds__(128) gotoh_warp_kernel(GotohJob job, GotohConst K) {
+    __shared__ uint32_t s_lut[10];
+    __shared__ int8_t s_lut25[32];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) s_lut[k] = K.lut4[k >> 1][k & 1];
+#pragma unroll
+        for (int k = 0; k < 25; k++) s_lut25[k] = K.lut[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp_slot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t *tb = job.tb + warp_slot * (job.tb_words + job.rb_words);
+    uint32_t *rb = tb + job.tb_words;
+    const uint64_t total = job.list_count ? (uint64_t)(*job.list_count) : job.n_pairs;
+    for (uint64_t k = warp_slot; k < total; k += n_warps) {
+        const uint32_t pi = job.list ? job.list[k] : (uint32_t)k;
+        PairSetup S;
+        if (!setup_pair(job, K, pi, job.tb_words, job.rb_words, lane == 0, S)) continue;
+        FillResult F = warp_fill(K, s_lut, S, tb, rb, lane);
+        __syncwarp();  // traceback words of every lane are visible to lane 0
+        if (lane == 0) finish_pair<1>(job, K, s_lut25, pi, S, F, tb);
+        __syncwarp();
+    }
+}
+
+cudaError_t launch_gotoh_warp(const GotohJob &job, const GotohConst &k, int warps,
+                              cudaStream_t st) {
+    int grid = (warps + 3) / 4;
+    gotoh_warp_kernel<<<grid, 128, 0, st>>>(job, k);
+    return cudaGetLastError();
 }
 
 int make_gotoh_const(const esp_extend_params &p, GotohConst &k) {

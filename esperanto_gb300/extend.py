@@ -95,6 +95,11 @@ class ExtendBuffer:
     def handle(self):
         return self._h
 
+    def set_warp_max(self, warp_max: int):
+        """Batches of at most warp_max pairs (and every per-call entry) run
+        one warp per pair, larger ones one thread per pair; same results."""
+        self.check(self._L.esp_set_warp_max(self._h, int(warp_max)))
+
     def stream_ptr(self) -> int:
         return self._L.esp_stream(self._h) or 0
 

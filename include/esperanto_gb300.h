@@ -86,6 +86,12 @@ typedef struct {
  * staging and grow-only device scratch).  Replaces the reference's
  * per-thread ExtendBuffer (crates/map/src/extend.rs:231-251). */
 int esp_create(esp_handle **out, int device);
+/* Kernel choice (no counterpart in the reference): batches of at most
+ * `warp_max` pairs -- every per-call entry point included -- run one warp per
+ * pair (a wavefront over the pair's strips); larger batches run one thread
+ * per pair in the persistent length-binned kernel.  Both give identical
+ * results.  Default 8192, or the ESP_WARP_MAX environment variable. */
+int esp_set_warp_max(esp_handle *h, long warp_max);
 int esp_destroy(esp_handle *h);
 /* Message of the last error on this handle (static storage of the handle). */
 const char *esp_last_error(const esp_handle *h);

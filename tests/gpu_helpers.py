@@ -1,4 +1,6 @@
 """Shared GPU-vs-oracle comparison helpers (the oracle is the checker)."""
+import functools
+
 import numpy as np
 
 import oracle as O
@@ -6,6 +8,7 @@ from esperanto_gb300 import batch as B
 from esperanto_gb300.extend import ExtendParams
 
 
+@functools.lru_cache(maxsize=None)
 def oracle_case(read, win, edit_dir, band, mode):
     """Oracle result of one case as (score, rs, re, fs, cigar, touch)."""
     p = O.Params(edit_dir=edit_dir)
@@ -16,7 +19,23 @@ def oracle_case(read, win, edit_dir, band, mode):
     return e.key(), t
 
 
-def gpu_batch(cases, edit_dir, mode=B.MODE_BAND, cigar_stride=None):
+_BUFS = {}
+
+
+def kernel_buffer(kind):
+    """A handle pinned to one DP kernel: 'warp' (warp per pair) or 'thread'
+    (thread per pair, length binned); None = the size-based default."""
+    if kind is None:
+        return None
+    if kind not in _BUFS:
+        from esperanto_gb300.extend import ExtendBuffer
+        b = ExtendBuffer()
+        b.set_warp_max(1 << 40 if kind == "warp" else 0)
+        _BUFS[kind] = b
+    return _BUFS[kind]
+
+
+def gpu_batch(cases, edit_dir, mode=B.MODE_BAND, cigar_stride=None, kernel=None):
     """cases: list of (read, win, band or None).  One batch per call."""
     reads = [c[0] for c in cases]
     wins = [c[1] for c in cases]
@@ -26,7 +45,7 @@ def gpu_batch(cases, edit_dir, mode=B.MODE_BAND, cigar_stride=None):
     if cigar_stride is None:
         cigar_stride = max(8, max(2 * (len(r) + len(w)) + 8 for r, w in zip(reads, wins)))
     out, cig = B.extend_batch_host(pairs, arena, n_iv, ExtendParams(edit_dir=edit_dir), mode,
-                                   cigar_stride)
+                                   cigar_stride, buf=kernel_buffer(kernel))
     res = []
     for k in range(len(cases)):
         o = out[k]
@@ -39,20 +58,28 @@ def gpu_batch(cases, edit_dir, mode=B.MODE_BAND, cigar_stride=None):
     return res
 
 
-def compare(cases, edit_dirs, mode=B.MODE_BAND, ctxs=None):
-    """Run cases grouped by edit_dir through GPU and oracle; assert equality."""
+def compare(cases, edit_dirs, mode=B.MODE_BAND, ctxs=None, kernels=("thread", "warp")):
+    """Run cases grouped by edit_dir through GPU (each DP kernel) and the
+    oracle; assert equality."""
+    n = 0
+    for kern in kernels:
+        n = _compare(cases, edit_dirs, mode, ctxs, kern)
+    return n
+
+
+def _compare(cases, edit_dirs, mode, ctxs, kernel):
     by_dir = {}
     for k, (c, d) in enumerate(zip(cases, edit_dirs)):
         by_dir.setdefault(d, []).append(k)
     n = 0
     for d, idx in by_dir.items():
-        got = gpu_batch([cases[k] for k in idx], d, mode)
+        got = gpu_batch([cases[k] for k in idx], d, mode, kernel=kernel)
         for k, g in zip(idx, got):
             read, win, band = cases[k]
             want, wt = oracle_case(read, win, d, band, mode)
             ctx = ctxs[k] if ctxs else str(k)
-            assert g[0] == want, f"{ctx}: gpu {g[0]} != oracle {want}"
+            assert g[0] == want, f"{ctx} [{kernel}]: gpu {g[0]} != oracle {want}"
             if wt is not None:
-                assert g[1] == wt, f"{ctx}: touch gpu {g[1]} != oracle {wt}"
+                assert g[1] == wt, f"{ctx} [{kernel}]: touch gpu {g[1]} != oracle {wt}"
             n += 1
     return n
