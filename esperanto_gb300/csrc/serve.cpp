@@ -37,6 +37,7 @@ struct Slot {
     esp_handle *h = nullptr;
     cudaEvent_t done = nullptr;
     Request *cur = nullptr;
+    int staged_rc = ESP_OK;      // launch() status of the current request
     uint8_t *h_stage = nullptr;  // pinned: pairs | n intervals | read arena | out | cigar
     uint8_t *d_stage = nullptr;
     size_t off_iv = 0, off_arena = 0, off_out = 0, off_cig = 0, bytes = 0;
@@ -107,9 +108,17 @@ int launch(esp_server *s, Slot &sl, Request *r) {
             uint32_t ws = (uint32_t)(pairs[i].win_pos - C.base), we = ws + pairs[i].win_len;
             pairs[i].n_first = (uint32_t)niv;
             uint32_t cnt = 0;
-            for (uint32_t k = 0; k < C.n_count; k++) {
-                const esp_n_interval &v = g->h_iv[C.n_first + k];
-                uint32_t a = std::max(v.start, ws), b = std::min(v.end, we);
+            // the contig's intervals are sorted and disjoint: start at the
+            // first one ending after the window start
+            const esp_n_interval *cv = g->h_iv.data() + C.n_first;
+            uint32_t lo = 0, hi = C.n_count;
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (cv[mid].end <= ws) lo = mid + 1;
+                else hi = mid;
+            }
+            for (uint32_t k = lo; k < C.n_count && cv[k].start < we; k++) {
+                uint32_t a = std::max(cv[k].start, ws), b = std::min(cv[k].end, we);
                 if (a < b) {
                     if (niv >= iv_cap) return ESP_EDOMAIN;
                     iv[niv++] = {a - ws, b - ws};
@@ -149,14 +158,18 @@ int launch(esp_server *s, Slot &sl, Request *r) {
     return ESP_OK;
 }
 
-void finish(esp_server *s, Slot &sl, int32_t status) {
+// Results of a finished slot into the caller's buffers (worker thread, no
+// lock held: the slot and its request belong to the worker until complete()).
+void copy_out(Slot &sl) {
+    const esp_serve_request &q = sl.cur->req;
+    memcpy(q.out, sl.h_stage + sl.off_out, q.n_reads * sizeof(esp_extension));
+    if (q.cigar && q.cigar_stride)
+        memcpy(q.cigar, sl.h_stage + sl.off_cig, q.n_reads * (size_t)q.cigar_stride * 4);
+}
+
+// Publish a slot's request as done (server lock held).
+void complete(esp_server *s, Slot &sl, int32_t status) {
     Request *r = sl.cur;
-    const esp_serve_request &q = r->req;
-    if (status == ESP_OK) {
-        memcpy(q.out, sl.h_stage + sl.off_out, q.n_reads * sizeof(esp_extension));
-        if (q.cigar && q.cigar_stride)
-            memcpy(q.cigar, sl.h_stage + sl.off_cig, q.n_reads * (size_t)q.cigar_stride * 4);
-    }
     r->status = status;
     r->latency_ms =
         std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count();
@@ -165,55 +178,64 @@ void finish(esp_server *s, Slot &sl, int32_t status) {
     sl.cur = nullptr;
 }
 
+// The worker owns the slots.  The server lock guards only the queue, the
+// ticket table and the budget: staging a request, launching it and copying
+// results out run unlocked, so submitters and waiters are never held up by
+// the bulk copies.
 void worker_loop(esp_server *s) {
     cudaSetDevice(s->device);
-    std::unique_lock<std::mutex> lk(s->mu);
+    std::vector<std::pair<Slot *, int32_t>> done;
+    std::vector<Slot *> to_launch;
     for (;;) {
-        bool any_done = false;
+        done.clear();
         for (Slot &sl : s->slots) {
-            if (!sl.cur) continue;
+            if (!sl.cur || sl.staged_rc != ESP_OK) continue;
             cudaError_t e = cudaEventQuery(sl.done);
             if (e == cudaErrorNotReady) continue;
-            finish(s, sl, e == cudaSuccess ? ESP_OK : ESP_ECUDA);
-            any_done = true;
+            if (e == cudaSuccess) copy_out(sl);
+            done.push_back({&sl, e == cudaSuccess ? ESP_OK : ESP_ECUDA});
         }
-        if (any_done) s->cv_done.notify_all();
-        // FIFO admission: the head request waits for a slot and for budget
-        while (!s->pending.empty()) {
-            Request *r = s->pending.front();
-            if (s->closing) {
+        to_launch.clear();
+        bool inflight = false, stop = false;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            for (Slot &sl : s->slots)  // launches that failed in the previous round
+                if (sl.cur && sl.staged_rc != ESP_OK) done.push_back({&sl, sl.staged_rc});
+            for (auto &d : done) complete(s, *d.first, d.second);
+            if (!done.empty()) s->cv_done.notify_all();
+            // FIFO admission: the head request waits for a slot and for budget
+            while (!s->pending.empty()) {
+                Request *r = s->pending.front();
+                if (s->closing) {
+                    s->pending.pop_front();
+                    r->status = ESP_ECLOSED;
+                    r->done = true;
+                    s->cv_done.notify_all();
+                    continue;
+                }
+                Slot *idle = nullptr;
+                for (Slot &sl : s->slots)
+                    if (!sl.cur) {
+                        idle = &sl;
+                        break;
+                    }
+                if (!idle || r->need > s->budget_free) break;
                 s->pending.pop_front();
-                r->status = ESP_ECLOSED;
-                r->done = true;
-                s->cv_done.notify_all();
+                s->budget_free -= r->need;
+                idle->cur = r;
+                idle->staged_rc = ESP_OK;
+                to_launch.push_back(idle);
+            }
+            for (Slot &sl : s->slots) inflight |= sl.cur != nullptr;
+            stop = s->stop && !inflight && s->pending.empty();
+            if (!stop && !inflight) {
+                s->cv_work.wait(lk);
                 continue;
             }
-            Slot *idle = nullptr;
-            for (Slot &sl : s->slots)
-                if (!sl.cur) {
-                    idle = &sl;
-                    break;
-                }
-            if (!idle || r->need > s->budget_free) break;
-            s->pending.pop_front();
-            s->budget_free -= r->need;
-            idle->cur = r;
-            int rc = launch(s, *idle, r);
-            if (rc != ESP_OK) {
-                finish(s, *idle, rc);
-                s->cv_done.notify_all();
-            }
         }
-        bool inflight = false;
-        for (Slot &sl : s->slots) inflight |= sl.cur != nullptr;
-        if (s->stop && !inflight && s->pending.empty()) break;
-        if (!inflight) {
-            s->cv_work.wait(lk);
-        } else {
-            lk.unlock();
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-            lk.lock();
-        }
+        if (stop) break;
+        for (Slot *sl : to_launch) sl->staged_rc = launch(s, *sl, sl->cur);
+        if (to_launch.empty()) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
