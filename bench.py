@@ -168,6 +168,19 @@ class GotohWorkload(Workload):
                              int(pairs["band_half"].max()))
         p = ExtendParams()._c()
         self._keep = (d_arena, d_pairs, d_out, d_cig, lim, p)
+        self.autotune = None
+        if n > 8192:
+            # pick the DP variant per length class on this batch (untimed);
+            # timed steps then replay one captured graph of the tuned launches
+            variants, ms = (C.c_int * 4)(), (C.c_double * 8)()
+            buf.check(L.esp_batch_autotune(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
+                                           d_arena.data_ptr(), arena.nbytes, None, 0,
+                                           C.byref(lim), C.byref(p), d_out.data_ptr(),
+                                           d_cig.data_ptr(), self.stride, None, variants, ms))
+            self.autotune = {"classes": ["w>=196", "100<=w<196", "52<=w<100", "w<52"],
+                             "variants": list(variants),
+                             "ms": [[round(ms[2 * s], 3), round(ms[2 * s + 1], 3)]
+                                    for s in range(4)]}
 
         def step():
             buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
@@ -609,6 +622,9 @@ def main():
         "clocks": clocks,
         "per_step_ms": per_step,
     }
+    if getattr(wl, "autotune", None):
+        line["config"]["autotune"] = wl.autotune
+        line["config"]["cuda_graph"] = "timed steps replay one captured graph"
     if config == 3:
         line["config"]["candidates"] = wl.n_cands
         line["config"]["rescued"] = wl.found

@@ -166,6 +166,9 @@ def lib():
                                     C.POINTER(vp)]
     L.esp_genome_destroy.argtypes = [vp]
     L.esp_set_warp_max.argtypes = [vp, C.c_long]
+    L.esp_batch_autotune.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                     C.c_uint64, C.POINTER(BatchLimitsC),
+                                     C.POINTER(ExtendParamsC), vp, vp, C.c_uint32, vp, vp, vp]
     L.esp_int_peaks.argtypes = [vp] + [C.POINTER(C.c_double)] * 4
     L.esp_paidx_scan.argtypes = [vp, C.c_uint64, C.POINTER(PaidxInfoC), C.c_char_p, sz]
     L.esp_paidx_contigs.argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint32, vp,

@@ -44,7 +44,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         if (mode == ESP_MODE_HINT &&
             (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
             return rc;
-        CK(h, cudaMemsetAsync(h->d_ctr, 0, 64, st));
+        CK(h, cudaMemsetAsync(h->d_ctr, 0, 256, st));
         esp::GotohJob job{};
         job.pairs = d_pairs;
         job.n_pairs = n_pairs;
@@ -85,9 +85,26 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         const char *v = getenv("ESP_GOTOH_VARIANT");
         h->variant = (v && *v == '0') ? 0 : 1;
     }
-    const int var = h->variant;
-    if (h->gotoh_bps[var] == 0) h->gotoh_bps[var] = esp::gotoh_blocks_per_sm(128, var);
-    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * h->gotoh_bps[var] * 4);
+    int var = h->variant;
+    // autotuned handle: one variant for every class runs as a single launch
+    bool tuned_split = false;
+    if (h->tuned) {
+        for (int s = 1; s < esp::kLengthClasses; s++) tuned_split |= h->tune[s] != h->tune[0];
+        if (!tuned_split && h->tune[0] >= 0) var = h->tune[0];
+    }
+    // the binned list runs per length class when the handle is autotuned (or
+    // is being tuned); scratch then covers the widest variant in use
+    const bool per_class = (tuned_split || h->autotune_ms) && h->binning && n_pairs > 32;
+    int max_bps = 0;
+    for (int v = 0; v < esp::kGotohVariants; v++) {
+        bool used = v == var;
+        if (per_class)
+            for (int s = 0; s < esp::kLengthClasses; s++) used |= h->autotune_ms || h->tune[s] == v;
+        if (!used) continue;
+        if (h->gotoh_bps[v] == 0) h->gotoh_bps[v] = esp::gotoh_blocks_per_sm(128, v);
+        max_bps = std::max(max_bps, h->gotoh_bps[v]);
+    }
+    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * max_bps * 4);
     uint64_t need_warps = (n_pairs + 31) / 32;
     uint64_t warps = std::min(want, need_warps);
     uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes);
@@ -100,7 +117,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     if (mode == ESP_MODE_HINT &&
         (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
         return rc;
-    CK(h, cudaMemsetAsync(h->d_ctr, 0, 64, st));
+    CK(h, cudaMemsetAsync(h->d_ctr, 0, 256, st));
     const uint32_t *order = nullptr;
     if (h->binning && n_pairs > 32) {
         if ((rc = grow_device(h, (void **)&h->d_hist, &h->d_hist_cap, esp::bin_scratch_bytes())) != ESP_OK)
@@ -108,8 +125,9 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         if ((rc = grow_device(h, (void **)&h->d_order, &h->d_order_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
             return rc;
         CK(h, esp::launch_binning(d_pairs, n_pairs, mode == ESP_MODE_HINT ? 1 : 0, h->d_hist,
-                                  h->d_order, h->num_sms, st));
-        h->launches += 3;
+                                  h->d_order, h->num_sms, st,
+                                  per_class ? h->d_ctr + 24 : nullptr));
+        h->launches += per_class ? 4 : 3;
         order = h->d_order;
     }
     esp::GotohJob job{};
@@ -134,8 +152,44 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     job.esc_count = h->d_ctr + 4;
     job.mode = mode == ESP_MODE_HINT ? 1 : 0;
     job.max_m = (int)L1.max_m;
-    CK(h, esp::launch_gotoh(job, K, (int)warps, 128, st, var));
-    h->launches++;
+    if (per_class && h->autotune_ms) {
+        // time every variant on every length class (best of two runs each);
+        // the batch's results are those of the last run of each class
+        cudaEvent_t ev[2];
+        CK(h, cudaEventCreate(&ev[0]));
+        CK(h, cudaEventCreate(&ev[1]));
+        for (int s = 0; s < esp::kLengthClasses; s++)
+            for (int v = 0; v < esp::kGotohVariants; v++) {
+                double best = 1e30;
+                for (int rep = 0; rep < 2; rep++) {
+                    esp::GotohJob js = job;
+                    js.range = h->d_ctr + 24 + s;
+                    js.queue = h->d_ctr + 8 + 2 * s;
+                    CK(h, cudaMemsetAsync(h->d_ctr + 8 + 2 * s, 0, 8, st));
+                    CK(h, cudaEventRecord(ev[0], st));
+                    CK(h, esp::launch_gotoh(js, K, (int)warps, 128, st, v));
+                    CK(h, cudaEventRecord(ev[1], st));
+                    CK(h, cudaEventSynchronize(ev[1]));
+                    float ms = 0;
+                    CK(h, cudaEventElapsedTime(&ms, ev[0], ev[1]));
+                    best = std::min(best, (double)ms);
+                }
+                h->autotune_ms[s * esp::kGotohVariants + v] = best;
+            }
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+    } else if (per_class) {
+        for (int s = 0; s < esp::kLengthClasses; s++) {
+            esp::GotohJob js = job;
+            js.range = h->d_ctr + 24 + s;
+            js.queue = h->d_ctr + 8 + 2 * s;
+            CK(h, esp::launch_gotoh(js, K, (int)warps, 128, st, h->tune[s] >= 0 ? h->tune[s] : var));
+            h->launches++;
+        }
+    } else {
+        CK(h, esp::launch_gotoh(job, K, (int)warps, 128, st, var));
+        h->launches++;
+    }
     if (mode == ESP_MODE_HINT) {
         esp::GotohJob j2 = job;
         j2.mode = 2;
@@ -187,7 +241,7 @@ int esp_create(esp_handle **out, int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_ctr, 64);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_ctr, 256);
     if (e != cudaSuccess) {
         delete h;
         return ESP_ECUDA;
@@ -206,6 +260,7 @@ int esp_destroy(esp_handle *h) {
     if (!h) return ESP_OK;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     cudaFree(h->d_in);
     cudaFree(h->d_res);
     cudaFree(h->d_tb);
@@ -429,8 +484,102 @@ int esp_batch_extend_device(esp_handle *h, int mode, const esp_pair *pairs, uint
                    limits->max_half < 0 ? -1 : limits->max_half);
     }
     cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
-    return enqueue_batch(h, mode, pairs, n_pairs, arena, arena_bytes, n_iv, n_iv_count, K, L1, L2,
-                         out, cigar, cigar_stride, st);
+    if (h->use_graphs < 0) {
+        const char *v = getenv("ESP_GRAPHS");
+        h->use_graphs = (v && *v == '0') ? 0 : 1;
+    }
+    auto run = [&]() {
+        return enqueue_batch(h, mode, pairs, n_pairs, arena, arena_bytes, n_iv, n_iv_count, K,
+                             L1, L2, out, cigar, cigar_stride, st);
+    };
+    if (!h->use_graphs || h->autotune_ms) return run();
+    // Repeated identical submissions (a resident batch re-run, a pipeline
+    // reusing its buffers) replay one captured graph: the first run grows the
+    // scratch, the second is captured, later ones launch the graph.
+    std::vector<uint64_t> key = {
+        (uint64_t)mode, (uint64_t)(uintptr_t)pairs, n_pairs, (uint64_t)(uintptr_t)arena,
+        arena_bytes, (uint64_t)(uintptr_t)n_iv, n_iv_count, limits->max_read_len,
+        limits->max_win_len, (uint64_t)(int64_t)limits->max_half, (uint64_t)params->match_score,
+        (uint64_t)params->mismatch, (uint64_t)params->gap_open, (uint64_t)params->gap_ext,
+        (uint64_t)params->edit_dir, (uint64_t)(uintptr_t)out, (uint64_t)(uintptr_t)cigar,
+        cigar_stride, (uint64_t)(uintptr_t)st, (uint64_t)h->warp_max, (uint64_t)h->variant,
+        (uint64_t)h->binning, (uint64_t)h->tuned};
+    for (int s = 0; s < esp::kLengthClasses; s++) key.push_back((uint64_t)(int64_t)h->tune[s]);
+    key.push_back(h->buf_gen);
+    if (h->graph_exec && key == h->graph_key) {
+        CK(h, cudaGraphLaunch(h->graph_exec, st));
+        h->launches = h->graph_launches;
+        return ESP_OK;
+    }
+    if (key != h->seen_key) {  // first sighting: run directly (grows scratch)
+        int rc = run();
+        key.back() = h->buf_gen;
+        h->seen_key = key;
+        return rc;
+    }
+    // second sighting with nothing regrown: capture, instantiate, launch
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+        h->graph_key.clear();
+    }
+    const uint64_t gen = h->buf_gen;
+    CK(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = run();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc != ESP_OK || e != cudaSuccess || h->buf_gen != gen) {
+        if (graph) cudaGraphDestroy(graph);
+        h->seen_key.clear();
+        if (rc != ESP_OK) return rc;
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+        return run();  // scratch moved during the capture: run directly
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    h->graph_exec = exec;
+    h->graph_key = key;
+    h->graph_launches = h->launches;
+    CK(h, cudaGraphLaunch(exec, st));
+    return ESP_OK;
+}
+
+int esp_batch_autotune(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
+                       const uint8_t *arena, uint64_t arena_bytes, const esp_n_interval *n_iv,
+                       uint64_t n_iv_count, const esp_batch_limits *limits,
+                       const esp_extend_params *params, esp_extension *out, uint32_t *cigar,
+                       uint32_t cigar_stride, void *stream, int *variants, double *ms) {
+    if (!h || !params || !out || !limits || !pairs || !arena) return fail(h, ESP_EINVAL, "null argument");
+    if (mode != ESP_MODE_BAND) return fail(h, ESP_EINVAL, "autotuning runs band-mode batches");
+    if (n_pairs <= (uint64_t)std::max<long>(32, h->warp_max < 0 ? 8192 : h->warp_max))
+        return fail(h, ESP_EINVAL, "autotuning needs a batch of the persistent kernel's size");
+    double t[esp::kLengthClasses * esp::kGotohVariants];
+    h->tuned = false;
+    h->autotune_ms = t;
+    int rc = esp_batch_extend_device(h, mode, pairs, n_pairs, arena, arena_bytes, n_iv,
+                                     n_iv_count, limits, params, out, cigar, cigar_stride, stream);
+    h->autotune_ms = nullptr;
+    if (rc != ESP_OK) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    CK(h, cudaStreamSynchronize(st));
+    for (int s = 0; s < esp::kLengthClasses; s++) {
+        int best = 0;
+        for (int v = 1; v < esp::kGotohVariants; v++)
+            if (t[s * esp::kGotohVariants + v] < t[s * esp::kGotohVariants + best]) best = v;
+        h->tune[s] = best;
+        if (variants) variants[s] = best;
+    }
+    if (ms) memcpy(ms, t, sizeof(t));
+    h->tuned = true;
+    h->seen_key.clear();  // launches differ from any captured graph
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+        h->graph_key.clear();
+    }
+    return ESP_OK;
 }
 
 }  // extern "C"

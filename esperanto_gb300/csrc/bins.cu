@@ -139,8 +139,21 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
 
 size_t bin_scratch_bytes() { return (size_t)NBINS * sizeof(uint32_t); }
 
+// Length classes of the binned list (descending cost): band/window width
+// w >= 196, [100, 196), [52, 100), < 52 columns.  bounds[s], bounds[s+1] is
+// class s; read from the scanned histogram before the scatter moves it.
+__global__ void class_bounds(const uint32_t *__restrict__ hist, uint64_t n,
+                             uint32_t *__restrict__ bounds) {
+    if (threadIdx.x == 0) {
+        const uint32_t first_key[3] = {(48u << 8) | 255u, (24u << 8) | 255u, (12u << 8) | 255u};
+        bounds[0] = 0;
+        for (int s = 0; s < 3; s++) bounds[s + 1] = hist[NBINS - 1 - first_key[s]];
+        bounds[4] = (uint32_t)n;
+    }
+}
+
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
-                           uint32_t *order, int num_sms, cudaStream_t st) {
+                           uint32_t *order, int num_sms, cudaStream_t st, uint32_t *bounds) {
     cudaError_t e = cudaMemsetAsync(hist, 0, bin_scratch_bytes(), st);
     if (e != cudaSuccess) return e;
     int grid = num_sms * 4;
@@ -148,6 +161,7 @@ cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t
     if ((uint64_t)grid > need) grid = (int)(need ? need : 1);
     bin_hist<<<grid, 256, 0, st>>>(pairs, n, mode, hist);
     bin_scan<<<1, 1024, 0, st>>>(hist);
+    if (bounds) class_bounds<<<1, 32, 0, st>>>(hist, n, bounds);
     bin_scatter<<<grid, 256, 0, st>>>(pairs, n, mode, hist, order);
     return cudaGetLastError();
 }

@@ -22,6 +22,14 @@ struct esp_handle {
     int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
     int variant = -1;   // DP kernel variant; -1 = ESP_GOTOH_VARIANT env or default
     long warp_max = -1; // batches of at most this many pairs run warp-per-pair; -1 = ESP_WARP_MAX or 8192
+    // CUDA graph of the last device batch: an identical submission (same
+    // buffers, sizes, parameters, stream, kernel choices and scratch
+    // generation) replays it instead of re-issuing its launches
+    uint64_t buf_gen = 0;
+    std::vector<uint64_t> graph_key, seen_key;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_launches = 0;
+    int use_graphs = -1;  // -1 = ESP_GRAPHS env (default on)
     uint64_t scratch_budget = 8ull << 30;  // bytes of DP scratch one launch may use
     // grow-only device buffers
     void *d_in = nullptr;       // per-call staging: pair | n intervals | arena
@@ -34,7 +42,12 @@ struct esp_handle {
     size_t d_rb_cap = 0;
     uint32_t *d_esc = nullptr;  // escalation list
     size_t d_esc_cap = 0;       // bytes
-    uint32_t *d_ctr = nullptr;  // [0..1] queues (u64), [4] esc count
+    // d_ctr (256 B): u64 queues at [0..1] (attempt 1), [2..3] (attempt 2),
+    // u32 esc count at [4], u64 class queues at [8..15], class bounds at [24..28]
+    uint32_t *d_ctr = nullptr;
+    int tune[esp::kLengthClasses] = {-1, -1, -1, -1};  // DP variant per length class (autotuned)
+    bool tuned = false;
+    double *autotune_ms = nullptr;  // set by esp_batch_autotune: time the classes instead
     uint32_t *d_hist = nullptr; // geometry bins
     size_t d_hist_cap = 0;
     uint32_t *d_order = nullptr;  // length-binned work list
@@ -78,6 +91,7 @@ inline int cuda_fail(esp_handle *h, cudaError_t e, const char *what) {
 
 inline int grow_device(esp_handle *h, void **p, size_t *cap, size_t need) {
     if (need <= *cap) return ESP_OK;
+    if (h) h->buf_gen++;  // buffers move: a captured launch graph is stale
     if (*p) cudaFree(*p);
     *p = nullptr;
     *cap = 0;

@@ -36,6 +36,7 @@ struct GotohJob {
     uint64_t n_pairs;
     const uint32_t *list;       // optional: indices into pairs (device); null = 0..n-1
     const uint32_t *list_count; // optional device counter (when list is a queue)
+    const uint32_t *range;      // optional device {begin, end}: items list[begin .. end)
     const uint8_t *arena;       // arena of the reads
     uint64_t arena_bases;       // bases addressable in it (excluding padding)
     const uint8_t *win_arena;   // arena of the windows (null = same as reads)
@@ -135,8 +136,11 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
 
 // Counting-sort the pairs by geometry (descending cost) into `order`.
 // `hist` needs bin_scratch_bytes() of device memory.  4 launches.
+// bounds (optional, 5 device words): the four length classes of the list.
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
-                           uint32_t *order, int num_sms, cudaStream_t st);
+                           uint32_t *order, int num_sms, cudaStream_t st,
+                           uint32_t *bounds = nullptr);
+constexpr int kLengthClasses = 4;
 size_t bin_scratch_bytes();
 
 // Traceback and row-buffer words one thread needs for a pair.

@@ -745,7 +745,11 @@ __global__ void __launch_bounds__(128, MINB) gotoh_kernel(GotohJob job, GotohCon
     const uint64_t warp_slot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t *tb = job.tb + warp_slot * job.tb_words * 32 + lane;
     uint32_t *rb = job.rb + warp_slot * job.rb_words * 32 + lane;
-    const uint64_t total = job.list_count ? (uint64_t)(*job.list_count) : job.n_pairs;
+    uint64_t b0 = 0, total = job.list_count ? (uint64_t)(*job.list_count) : job.n_pairs;
+    if (job.range) {  // one length class of the binned list
+        b0 = job.range[0];
+        total = job.range[1] > job.range[0] ? job.range[1] - job.range[0] : 0;
+    }
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd((unsigned long long *)job.queue, 32ull);
@@ -753,7 +757,7 @@ __global__ void __launch_bounds__(128, MINB) gotoh_kernel(GotohJob job, GotohCon
         if (base >= total) break;
         uint64_t k = base + lane;
         if (k < total) {
-            uint32_t pi = job.list ? job.list[k] : (uint32_t)k;
+            uint32_t pi = job.list ? job.list[b0 + k] : (uint32_t)(b0 + k);
             process_pair(job, K, s_lut, s_lut25, pi, tb, rb);
         }
     }

@@ -183,6 +183,21 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
                           const esp_extend_params *params, esp_extension *out,
                           uint32_t *cigar, uint32_t cigar_stride);
 
+/* Autotuning per length class (no counterpart in the reference): runs the
+ * band-mode batch once per DP kernel variant on each of four length classes
+ * of its binned work list (band/window width >= 196, [100, 196), [52, 100),
+ * < 52 columns), keeps the fastest variant per class for every later batch
+ * of the handle (ms: 8 timings, class-major over the two variants -- 168
+ * registers and 3 blocks per SM, 128 registers and 4 blocks per SM;
+ * variants: the choice per class; either may be null) and leaves the batch's
+ * results in out/cigar.
+ * Needs a batch above the warp-per-pair size. */
+int esp_batch_autotune(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
+                       const uint8_t *arena, uint64_t arena_bytes, const esp_n_interval *n_iv,
+                       uint64_t n_iv_count, const esp_batch_limits *limits,
+                       const esp_extend_params *params, esp_extension *out, uint32_t *cigar,
+                       uint32_t cigar_stride, void *stream, int *variants, double *ms);
+
 /* ---- EA-Myers filters: crates/map/src/myers_ea.rs, crates/engine/src/myers.rs ----
  *
  * Editing-aware equality: read A matches reference {A}, C matches {C,T},
