@@ -166,6 +166,13 @@ def lib():
                                     C.POINTER(vp)]
     L.esp_genome_destroy.argtypes = [vp]
     L.esp_set_warp_max.argtypes = [vp, C.c_long]
+    L.esp_intron_length_penalty.argtypes = [C.c_uint32]
+    L.esp_intron_length_penalty.restype = C.c_int32
+    L.esp_batch_rescore_host.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64,
+                                         vp, C.c_uint64, C.POINTER(ExtendParamsC), vp, vp]
+    L.esp_batch_rescore_device.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                           C.c_uint64, vp, C.c_uint64,
+                                           C.POINTER(ExtendParamsC), vp, vp, vp]
     L.esp_batch_autotune.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
                                      C.c_uint64, C.POINTER(BatchLimitsC),
                                      C.POINTER(ExtendParamsC), vp, vp, C.c_uint32, vp, vp, vp]

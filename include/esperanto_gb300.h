@@ -417,6 +417,47 @@ int esp_batch_splice_device(esp_handle *h, const esp_genome *g, const esp_splice
 /* DP cells of the last batch splice call (both extension attempts counted). */
 uint64_t esp_last_cells(const esp_handle *h);
 
+/* ---- strict rescoring: crates/map/src/align.rs:1060-1165 rescore_with ----
+ *
+ * One record per placement: its query (ASCII, compared byte for byte as the
+ * reference does), contig, start and CIGAR (u32 len<<4|op, ESP_OP_*), and the
+ * editing direction exempted from the mismatch charge.  `lib` is the
+ * junction library sorted by (contig, start, end) (JunctionLib, gtf.rs;
+ * minus_strand ignored: contains_any_strand).  sp = null uses
+ * SpliceParams::default() as rescore_with does. */
+typedef struct {
+    uint64_t query_pos;  /* byte offset of the query in the query arena */
+    uint32_t query_len;
+    uint32_t contig;
+    uint32_t pos;        /* placement start on the contig */
+    uint32_t op_first;   /* first CIGAR op in the op array */
+    uint32_t op_count;
+    int32_t edit_dir;    /* ESP_EDIT_* */
+} esp_rescore_item;
+
+typedef struct {         /* align.rs:188-211 StrictScore */
+    int32_t score;
+    uint32_t aligned, matches, mm, ea_ag, ea_tc, ins, del, clipped, n_splice;
+    int32_t splice_score;
+    int32_t status;      /* ESP_OK, or ESP_EINVAL for a record outside its tables */
+} esp_strict_score;
+
+/* splice.rs:119-121 intron_length_penalty through the threshold table the
+ * rescoring kernel uses (host-side; equal to the reference's f64 formula for
+ * every u32 length). */
+int32_t esp_intron_length_penalty(uint32_t len);
+
+int esp_batch_rescore_device(esp_handle *h, const esp_genome *g, const esp_rescore_item *items,
+                             uint64_t n, const uint8_t *queries, uint64_t query_bytes,
+                             const uint32_t *ops, uint64_t n_ops, const esp_junction *lib,
+                             uint64_t n_lib, const esp_extend_params *params,
+                             const esp_splice_params *sp, esp_strict_score *out, void *stream);
+int esp_batch_rescore_host(esp_handle *h, const esp_genome *g, const esp_rescore_item *items,
+                           uint64_t n, const uint8_t *queries, uint64_t query_bytes,
+                           const uint32_t *ops, uint64_t n_ops, const esp_junction *lib,
+                           uint64_t n_lib, const esp_extend_params *params,
+                           const esp_splice_params *sp, esp_strict_score *out);
+
 /* ---- serving loop (new): continuous batching over a resident genome ----
  *
  * A server owns `n_streams` in-flight slots, each a CUDA stream with its own

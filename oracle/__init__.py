@@ -22,7 +22,7 @@ from typing import List, Optional, Sequence, Tuple
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libesp_oracle.so")
-SOURCES = ["extend.c", "myers.c", "split.c", "batch.c"]
+SOURCES = ["extend.c", "myers.c", "split.c", "batch.c", "rescore.c"]
 
 OP_M, OP_I, OP_D, OP_N, OP_S = 0, 1, 2, 3, 4
 OP_CHARS = "MIDNS"
@@ -38,7 +38,7 @@ def build(force: bool = False) -> str:
         if all(os.path.getmtime(s) <= lib_m for s in srcs):
             return LIB_PATH
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
-           "-o", LIB_PATH + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES]
+           "-o", LIB_PATH + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES] + ["-lm"]
     subprocess.run(cmd, check=True)
     os.replace(LIB_PATH + ".tmp", LIB_PATH)
     return LIB_PATH
@@ -555,3 +555,41 @@ def batch_channel_a(garena, contigs, read_ascii, read_off, reads, cands, threads
     if rc != 0:
         raise OracleError(f"orc_batch_channel_a returned {rc}")
     return found, score, cells.value
+
+
+class _Strict(C.Structure):
+    _fields_ = [("score", C.c_int32), ("aligned", C.c_uint32), ("matches", C.c_uint32),
+                ("mm", C.c_uint32), ("ea_ag", C.c_uint32), ("ea_tc", C.c_uint32),
+                ("ins", C.c_uint32), ("del_", C.c_uint32), ("clipped", C.c_uint32),
+                ("n_splice", C.c_uint32), ("splice_score", C.c_int32)]
+
+
+STRICT_FIELDS = ("score", "aligned", "matches", "mm", "ea_ag", "ea_tc", "ins", "del_", "clipped",
+                 "n_splice", "splice_score")
+
+
+def intron_length_penalty(n: int) -> int:
+    """splice.rs:119-121 (host libm log10)."""
+    f = lib().orc_intron_length_penalty
+    f.restype = C.c_int32
+    f.argtypes = [C.c_uint32]
+    return f(n)
+
+
+def rescore(contig: "Contig", contig_id: int, pos: int, query, ops, junction_lib=(),
+            params: Params = Params(), edit_dir: int = 0):
+    """align.rs:1060-1165 rescore_with: the StrictScore of a placement as a
+    tuple in STRICT_FIELDS order.  ops: u32 (len << 4 | op), M I D N S = 0..4;
+    junction_lib: (contig, start, end) sorted."""
+    q = _b(query)
+    arr = (C.c_uint32 * max(1, len(ops)))(*ops)
+    flat = [v for j in junction_lib for v in j]
+    jl = (C.c_uint32 * max(1, len(flat)))(*flat)
+    s = _Strict()
+    f = lib().orc_rescore
+    f.restype = None
+    f.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_char_p, C.c_uint32, C.c_void_p,
+                  C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int, C.c_void_p]
+    f(C.byref(contig.c), contig_id, pos, q, len(q), arr, len(ops), jl, len(junction_lib),
+      C.byref(params.c()), edit_dir, C.byref(s))
+    return tuple(getattr(s, k) for k in STRICT_FIELDS)

@@ -170,6 +170,20 @@ int orc_channel_a(const orc_contig *c, const uint8_t *read, uint32_t read_len,
                   const uint32_t *support, uint32_t n_cands, const orc_splice_params *sp,
                   const orc_params *p, orc_rescue *out);
 
+/* ---- strict rescoring, crates/map/src/align.rs:1060-1165 ---- */
+typedef struct {
+    uint32_t contig, start, end;   /* JunctionLib entry, (contig, start, end)-sorted */
+} orc_lib_junction;
+typedef struct {                   /* align.rs:188-211 StrictScore */
+    int32_t score;
+    uint32_t aligned, matches, mm, ea_ag, ea_tc, ins, del, clipped, n_splice;
+    int32_t splice_score;
+} orc_strict;
+int32_t orc_intron_length_penalty(uint32_t len);
+void orc_rescore(const orc_contig *c, uint32_t contig_id, uint32_t pos, const uint8_t *query,
+                 uint32_t qlen, const uint32_t *ops, uint32_t n_ops, const orc_lib_junction *lib,
+                 uint64_t n_lib, const orc_params *p, int dir, orc_strict *s);
+
 /* ---- batch drivers for the CPU baseline (one worker per thread, like the
  * reference's rayon map_init over per-thread buffers) ---- */
 typedef struct {
