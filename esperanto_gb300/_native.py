@@ -166,6 +166,9 @@ def lib():
                                     C.POINTER(vp)]
     L.esp_genome_destroy.argtypes = [vp]
     L.esp_set_warp_max.argtypes = [vp, C.c_long]
+    L.esp_batch_spliced_host.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                         C.c_uint64, vp, C.c_uint64, C.POINTER(ExtendParamsC),
+                                         vp, vp, vp, C.c_uint32]
     L.esp_intron_length_penalty.argtypes = [C.c_uint32]
     L.esp_intron_length_penalty.restype = C.c_int32
     L.esp_batch_rescore_host.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64,

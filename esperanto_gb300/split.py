@@ -7,6 +7,9 @@ the GB300 kernels, plus the resident genome it reads windows from.
 * ``channel_a_batch``   -- channel A (split.rs:468-570) over many reads, each
                            with its library candidates, + build_rescue_ext.
 * ``score_tail_win``    -- splice.rs:667-684; ``tail_gate`` splice.rs:705-708.
+* ``align_spliced``     -- splice.rs:617-664 on given exon slices: the DP on
+                           the device-gathered pseudo-reference, stitch_cigar
+                           (:435-493) and genomic_start (:414-424).
 * ``paidx_contigs``     -- the contigs of a paidx v1 index (index_io.rs),
                            validated as the reference's loader does;
                            ``Genome.from_paidx`` makes them resident.
@@ -146,6 +149,64 @@ class Genome:
             self.close()
         except Exception:
             pass
+
+
+SPLICED_READ_DTYPE = np.dtype([("read_pos", "<u8"), ("read_len", "<u4"), ("contig", "<u4"),
+                               ("exon_first", "<u4"), ("exon_count", "<u4"),
+                               ("n_first", "<u4"), ("n_read", "<u4")])
+EXON_DTYPE = np.dtype([("start", "<u4"), ("end", "<u4")])
+SPLICED_RES_DTYPE = np.dtype([("ext", B.EXT_DTYPE), ("genomic_start", "<u4"), ("n_ops", "<u4"),
+                              ("status", "<i4"), ("pad", "<u4")])
+
+
+def align_spliced_batch(genome: Genome, reads: Sequence, contigs: Sequence[int],
+                        exon_lists: Sequence[Sequence[Tuple[int, int]]],
+                        params: ExtendParams = ExtendParams(), cigar_stride: int = 64,
+                        buf: Optional[ExtendBuffer] = None):
+    """align_spliced for many reads, each with its contig and exon slices
+    [(start, end)]: (SPLICED_RES_DTYPE records, extension CIGARs, stitched
+    CIGARs), the CIGARs as (n, cigar_stride) u32 arrays."""
+    buf = buf or _default_buffer()
+    n = len(reads)
+    reads = [_b(r) for r in reads]
+    arena, pairs, n_iv = B.pack_ascii_pairs(reads, [b""] * n, [0] * n, [-1] * n)
+    R = np.zeros(n, SPLICED_READ_DTYPE)
+    ex = []
+    for k in range(n):
+        R[k] = (pairs["read_pos"][k], pairs["read_len"][k], contigs[k], len(ex),
+                len(exon_lists[k]), pairs["n_first"][k], pairs["n_read"][k])
+        ex.extend(exon_lists[k])
+    E = np.array(ex, np.uint32).reshape(-1, 2).view(EXON_DTYPE).reshape(-1) if ex else \
+        np.zeros(0, EXON_DTYPE)
+    E = np.ascontiguousarray(E)
+    out = np.zeros(n, SPLICED_RES_DTYPE)
+    ecig = np.zeros((max(1, n), cigar_stride), np.uint32)
+    scig = np.zeros((max(1, n), cigar_stride), np.uint32)
+    p = params._c()
+    niv = np.ascontiguousarray(n_iv, B.NIV_DTYPE)
+    rc = N.lib().esp_batch_spliced_host(buf.handle, genome.handle, R.ctypes.data, n,
+                                        arena.ctypes.data, len(arena),
+                                        niv.ctypes.data if len(niv) else None, len(niv),
+                                        E.ctypes.data if len(E) else None, len(E), C.byref(p),
+                                        out.ctypes.data, ecig.ctypes.data, scig.ctypes.data,
+                                        cigar_stride)
+    buf.check(rc)
+    return out, ecig[:n], scig[:n]
+
+
+def align_spliced(genome: Genome, read, contig: int, exons: Sequence[Tuple[int, int]],
+                  params: ExtendParams = ExtendParams(), buf: Optional[ExtendBuffer] = None):
+    """One read: (Extension against the pseudo-reference, stitched CIGAR as
+    [(op, len)], genomic start)."""
+    stride = 2 * (len(_b(read)) + sum(e - s for s, e in exons)) + 2 * len(exons) + 8
+    out, ecig, scig = align_spliced_batch(genome, [read], [contig], [exons], params, stride, buf)
+    o = out[0]
+    if o["status"] != 0:
+        raise N.EspError(int(o["status"]), "align_spliced failed")
+    x = o["ext"]
+    ext = Extension(int(x["read_start"]), int(x["read_end"]), int(x["ref_start"]),
+                    decode_cigar(ecig[0][:int(x["n_ops"])]), int(x["score"]))
+    return ext, decode_cigar(scig[0][:int(o["n_ops"])]), int(o["genomic_start"])
 
 
 class PaidxError(ValueError):

@@ -417,6 +417,45 @@ int esp_batch_splice_device(esp_handle *h, const esp_genome *g, const esp_splice
 /* DP cells of the last batch splice call (both extension attempts counted). */
 uint64_t esp_last_cells(const esp_handle *h);
 
+/* ---- spliced pseudo-reference DP: crates/map/src/splice.rs align_spliced ----
+ *
+ * align_spliced (splice.rs:617-664) after prepare_spliced chose the exon
+ * slices (refinement and guards upstream): the read (2-bit arena + N
+ * intervals) is extended with extend_hint along the direct diagonal against
+ * the concatenation of its slices [start, end) of its contig (gathered on the
+ * device from the resident genome), and the CIGAR is stitched back to the
+ * genome (stitch_cigar, :435-493) with an intron of exons[i+1].start -
+ * exons[i].end at every seam; genomic_start (:414-424) maps the pseudo start
+ * back.  CIGARs go to fixed-stride arrays. */
+typedef struct {
+    uint64_t read_pos;    /* base offset in the read arena */
+    uint32_t read_len;
+    uint32_t contig;
+    uint32_t exon_first;  /* first slice of this read in the exon table */
+    uint32_t exon_count;  /* >= 1, ascending and disjoint */
+    uint32_t n_first;     /* the read's N intervals */
+    uint32_t n_read;
+} esp_spliced_read;
+
+typedef struct {
+    uint32_t start, end;  /* genomic [start, end) on the read's contig */
+} esp_exon;
+
+typedef struct {
+    esp_extension ext;     /* extension against the pseudo-reference */
+    uint32_t genomic_start;
+    uint32_t n_ops;        /* stitched CIGAR ops */
+    int32_t status;        /* ESP_OK, or ESP_ECAP when a CIGAR exceeds the stride */
+    uint32_t pad;
+} esp_spliced_result;
+
+int esp_batch_spliced_host(esp_handle *h, const esp_genome *g, const esp_spliced_read *reads,
+                           uint64_t n, const uint8_t *read_arena, uint64_t read_arena_bytes,
+                           const esp_n_interval *read_iv, uint64_t n_read_iv,
+                           const esp_exon *exons, uint64_t n_exons,
+                           const esp_extend_params *params, esp_spliced_result *out,
+                           uint32_t *ext_cigar, uint32_t *stitched_cigar, uint32_t cigar_stride);
+
 /* ---- strict rescoring: crates/map/src/align.rs:1060-1165 rescore_with ----
  *
  * One record per placement: its query (ASCII, compared byte for byte as the

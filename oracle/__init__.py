@@ -22,7 +22,7 @@ from typing import List, Optional, Sequence, Tuple
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libesp_oracle.so")
-SOURCES = ["extend.c", "myers.c", "split.c", "batch.c", "rescore.c"]
+SOURCES = ["extend.c", "myers.c", "split.c", "batch.c", "rescore.c", "spliced.c"]
 
 OP_M, OP_I, OP_D, OP_N, OP_S = 0, 1, 2, 3, 4
 OP_CHARS = "MIDNS"
@@ -99,8 +99,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
+        build()  # no-op when the library is newer than every source
         L = C.CDLL(LIB_PATH)
         u8p = C.c_char_p
         i64, i32 = C.c_int64, C.c_int32
@@ -593,3 +592,43 @@ def rescore(contig: "Contig", contig_id: int, pos: int, query, ops, junction_lib
     f(C.byref(contig.c), contig_id, pos, q, len(q), arr, len(ops), jl, len(junction_lib),
       C.byref(params.c()), edit_dir, C.byref(s))
     return tuple(getattr(s, k) for k in STRICT_FIELDS)
+
+
+def stitch_cigar(ops, p_start: int, bounds, junction_lens):
+    """splice.rs:435-493; bounds [(pseudo_start, ref_start, ref_end)],
+    junction_lens[i] = intron length of junction i; ops u32 (len << 4 | op)."""
+    flat = [v for b in bounds for v in b]
+    a = (C.c_uint32 * max(1, len(ops)))(*ops)
+    bb = (C.c_uint32 * max(1, len(flat)))(*flat)
+    jl = (C.c_uint32 * max(1, len(junction_lens)))(*junction_lens)
+    cap = 2 * len(ops) + 2 * len(bounds) + 8
+    out = (C.c_uint32 * cap)()
+    f = lib().orc_stitch_cigar
+    f.restype = C.c_uint32
+    f.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                  C.c_uint32, C.c_void_p, C.c_uint32]
+    n = f(a, len(ops), p_start, bb, len(bounds), jl, len(junction_lens), out, cap)
+    return list(out[:n])
+
+
+def align_spliced_exons(contig: "Contig", read, exons, params: Params = Params()):
+    """align_spliced (splice.rs:617-664) on the exon slices [(rs, re)]:
+    (Ext against the pseudo-reference, stitched ops, genomic start)."""
+    r = _b(read)
+    total = sum(e - s for s, e in exons)
+    flat = [v for x in exons for v in x]
+    ex = (C.c_uint32 * max(1, len(flat)))(*flat)
+    cap = 2 * (len(r) + total) + 8
+    buf = (C.c_uint32 * cap)()
+    e = _Ext(0, 0, 0, 0, 0, cap, buf)
+    st = (C.c_uint32 * (cap + 2 * len(exons)))()
+    ns, gs = C.c_uint32(), C.c_uint32()
+    f = lib().orc_align_spliced_exons
+    f.argtypes = [C.c_void_p, C.c_char_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    rc = f(C.byref(contig.c), r, len(r), ex, len(exons), C.byref(params.c()), C.byref(e), st,
+           cap + 2 * len(exons), C.byref(ns), C.byref(gs))
+    if rc != 0:
+        raise OracleError(f"orc_align_spliced_exons returned {rc}")
+    ext = Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops]))
+    return ext, list(st[:ns.value]), gs.value

@@ -170,6 +170,16 @@ int orc_channel_a(const orc_contig *c, const uint8_t *read, uint32_t read_len,
                   const uint32_t *support, uint32_t n_cands, const orc_splice_params *sp,
                   const orc_params *p, orc_rescue *out);
 
+/* ---- spliced pseudo-reference DP, crates/map/src/splice.rs ---- */
+uint32_t orc_stitch_cigar(const uint32_t *ops, uint32_t n_ops, uint32_t p_start,
+                          const uint32_t *bounds, uint32_t n_bounds, const uint32_t *jlen,
+                          uint32_t n_j, uint32_t *out, uint32_t cap);
+uint32_t orc_genomic_start(uint32_t p, const uint32_t *bounds, uint32_t n_bounds);
+int orc_align_spliced_exons(const orc_contig *c, const uint8_t *read, uint32_t m,
+                            const uint32_t *exons, uint32_t n_exons, const orc_params *p,
+                            orc_ext *ext, uint32_t *stitched, uint32_t cap,
+                            uint32_t *n_stitched, uint32_t *gstart);
+
 /* ---- strict rescoring, crates/map/src/align.rs:1060-1165 ---- */
 typedef struct {
     uint32_t contig, start, end;   /* JunctionLib entry, (contig, start, end)-sorted */

@@ -167,3 +167,45 @@ def test_genome_from_paidx_matches_sequences():
                 (a2.dro, a2.left_win_lo, a2.total, a2.left.key(), a2.right.key())
             n += 1
     assert n > 10
+
+
+def test_align_spliced_vs_oracle():
+    """align_spliced on given exon slices (pseudo-reference gathered on the
+    device, extend_hint, stitch_cigar, genomic_start) against the oracle."""
+    rng = random.Random(0x5E11)
+    seqs = [_rand_contig(rng, n, 8) for n in (30000, 12000)]
+    g = S.Genome.from_sequences(seqs)
+    oc = [O.Contig(s) for s in seqs]
+    reads, cs, exl = [], [], []
+    for _ in range(400):
+        c = rng.randrange(2)
+        L = len(seqs[c])
+        k = rng.randrange(1, 5)
+        pos, exons = rng.randrange(100, 2000), []
+        for _ in range(k):  # ascending, disjoint slices with introns between
+            ln = rng.randrange(15, 90)
+            exons.append((pos, pos + ln))
+            pos += ln + rng.randrange(1, 3000)
+        if exons[-1][1] > L:
+            continue
+        body = bytearray(b"".join(seqs[c][s:e] for s, e in exons))
+        for q in range(len(body)):  # errors and N
+            if rng.random() < 0.03:
+                body[q] = rng.choice(b"ACGTN")
+        lo, hi = rng.randrange(0, 8), rng.randrange(0, 8)
+        read = bytes(body[lo:len(body) - hi]) or b"A"
+        reads.append(read)
+        cs.append(c)
+        exl.append(exons)
+    out, ecig, scig = S.align_spliced_batch(g, reads, cs, exl, cigar_stride=256)
+    assert (out["status"] == 0).all()
+    for k in range(len(reads)):
+        ext, st, gs = O.align_spliced_exons(oc[cs[k]], reads[k], exl[k])
+        o = out[k]
+        x = o["ext"]
+        got = (int(x["score"]), int(x["read_start"]), int(x["read_end"]), int(x["ref_start"]),
+               tuple(B.cigar_of(ecig[k], int(x["n_ops"]))))
+        assert got == ext.key(), (k, exl[k])
+        assert list(scig[k][:int(o["n_ops"])]) == st, (k, exl[k])
+        assert int(o["genomic_start"]) == gs
+    assert len(reads) > 300
