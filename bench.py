@@ -169,7 +169,7 @@ class GotohWorkload(Workload):
         p = ExtendParams()._c()
         self._keep = (d_arena, d_pairs, d_out, d_cig, lim, p)
         self.autotune = None
-        if n > 8192:
+        if n > 2048:
             # pick the DP variant per length class on this batch (untimed);
             # timed steps then replay one captured graph of the tuned launches
             variants, ms = (C.c_int * 4)(), (C.c_double * 8)()

@@ -28,7 +28,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     int rc;
     if (h->warp_max < 0) {
         const char *v = getenv("ESP_WARP_MAX");
-        h->warp_max = v ? atol(v) : 8192;
+        h->warp_max = v ? atol(v) : 2048;
     }
     if (n_pairs <= (uint64_t)h->warp_max) {
         // Few pairs: one warp per pair (the wavefront kernel), so a lone
@@ -553,7 +553,7 @@ int esp_batch_autotune(esp_handle *h, int mode, const esp_pair *pairs, uint64_t 
                        uint32_t cigar_stride, void *stream, int *variants, double *ms) {
     if (!h || !params || !out || !limits || !pairs || !arena) return fail(h, ESP_EINVAL, "null argument");
     if (mode != ESP_MODE_BAND) return fail(h, ESP_EINVAL, "autotuning runs band-mode batches");
-    if (n_pairs <= (uint64_t)std::max<long>(32, h->warp_max < 0 ? 8192 : h->warp_max))
+    if (n_pairs <= (uint64_t)std::max<long>(32, h->warp_max < 0 ? 2048 : h->warp_max))
         return fail(h, ESP_EINVAL, "autotuning needs a batch of the persistent kernel's size");
     double t[esp::kLengthClasses * esp::kGotohVariants];
     h->tuned = false;

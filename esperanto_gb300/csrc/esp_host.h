@@ -21,7 +21,7 @@ struct esp_handle {
     uint64_t launches = 0;
     int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
     int variant = -1;   // DP kernel variant; -1 = ESP_GOTOH_VARIANT env or default
-    long warp_max = -1; // batches of at most this many pairs run warp-per-pair; -1 = ESP_WARP_MAX or 8192
+    long warp_max = -1; // batches of at most this many pairs run warp-per-pair; -1 = ESP_WARP_MAX or 2048
     // CUDA graph of the last device batch: an identical submission (same
     // buffers, sizes, parameters, stream, kernel choices and scratch
     // generation) replays it instead of re-issuing its launches

@@ -830,14 +830,23 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
             diag = (int)(rb[clo - 1 - plo] & 0xffffu);
         uint32_t *tbs = tb + (size_t)s * sw;
         const bool handoff = lane == 31 && s + 1 < nstrips;
+        int cw_at = -1000000;  // first window position of the cached code word
+        uint32_t cw = 0, cn = 0;
         for (int t = t0; t <= t1; t++) {
             uint32_t in = __shfl_up_sync(0xffffffffu, pub, 1);
             const int j = t - lane;
             if (lane == 0) in = (base && j >= plo && j <= phi) ? rb[j - plo] : ABSENT;
             uint32_t out = ABSENT;
             if (act && j >= clo && j <= chi) {
-                uint32_t code = P.win.cnt ? P.win.code(j - 1)
-                                          : load1(P.win.arena, P.win.pos + (uint64_t)(j - 1));
+                // window codes 16 at a time (a load per column would sit on
+                // the wavefront's critical path)
+                if (j - 1 >= cw_at + 16) {
+                    cw_at = j - 1;
+                    cw = load16(P.win.arena, P.win.pos + (uint64_t)cw_at);
+                    cn = P.win.cnt ? nmask16(P.win.iv, P.win.cnt, cw_at) : 0u;
+                }
+                const int sh = j - 1 - cw_at;
+                uint32_t code = ((cn >> (31 - sh)) & 1u) ? 4u : ((cw >> (30 - 2 * sh)) & 3u);
                 uint32_t sel = code * 0x1111u + 0x8880u;
                 int upH = (int)(in & 0xffffu), upE = ((int)in) >> 16;
                 uint32_t word = dp_column<1>(S, K, j, sel, 32767u - (uint32_t)j, upH, upE, diag);

@@ -90,7 +90,7 @@ int esp_create(esp_handle **out, int device);
  * `warp_max` pairs -- every per-call entry point included -- run one warp per
  * pair (a wavefront over the pair's strips); larger batches run one thread
  * per pair in the persistent length-binned kernel.  Both give identical
- * results.  Default 8192, or the ESP_WARP_MAX environment variable. */
+ * results.  Default 2048, or the ESP_WARP_MAX environment variable. */
 int esp_set_warp_max(esp_handle *h, long warp_max);
 int esp_destroy(esp_handle *h);
 /* Message of the last error on this handle (static storage of the handle). */
