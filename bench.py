@@ -169,7 +169,7 @@ class GotohWorkload(Workload):
         p = ExtendParams()._c()
         self._keep = (d_arena, d_pairs, d_out, d_cig, lim, p)
         self.autotune = None
-        if n > 2048:
+        if n > 2048 and not getattr(self, "no_autotune", False):
             # pick the DP variant per length class on this batch (untimed);
             # timed steps then replay one captured graph of the tuned launches
             variants, ms = (C.c_int * 4)(), (C.c_double * 8)()
@@ -505,6 +505,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the per-length-class kernel autotuning (profiling runs)")
     args = ap.parse_args()
     rank, world, local = dist_init(args)
     config = args.config
@@ -516,6 +518,7 @@ def main():
     seed = SEEDS[config] + 1000 * rank  # weak scaling: each rank runs its own batch
     threads = os.cpu_count() or 1
     wl = make_workload(config)
+    wl.no_autotune = args.no_autotune
 
     if args.impl == "reference":
         if rank == 0:
