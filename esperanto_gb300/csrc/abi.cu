@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "esp_host.h"
@@ -261,6 +262,7 @@ int esp_destroy(esp_handle *h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     cudaFree(h->d_in);
     cudaFree(h->d_res);
     cudaFree(h->d_tb);
@@ -401,18 +403,60 @@ int esp_run_band(esp_handle *h, const uint8_t *read, size_t read_len, const uint
                     band_half < 0 ? 0 : band_offset, band_half, out, cigar, cigar_cap);
 }
 
-static int batch_common(esp_handle *h, int mode, const esp_pair *pairs_host, uint64_t n_pairs,
-                        Limits &L1, Limits &L2) {
-    for (uint64_t k = 0; k < n_pairs; k++) {
-        const esp_pair &P = pairs_host[k];
+// Scratch limits of a host batch (and, per chunk, the highest arena base
+// its pairs touch).  Large batches are scanned by several host threads: one
+// core streams ~8 GB/s, the 40-byte records of millions of pairs would
+// otherwise dominate the end-to-end time.
+struct ScanOut {
+    Limits L1, L2;
+    uint64_t arena_end = 0;
+};
+
+static void scan_range(int mode, const esp_pair *pairs, uint64_t a, uint64_t b, ScanOut &S) {
+    for (uint64_t k = a; k < b; k++) {
+        const esp_pair &P = pairs[k];
         if (mode == ESP_MODE_HINT) {
-            add_limits(L1, P.read_len, P.win_len, P.win_len <= 30 ? -1 : 30);
-            add_limits(L2, P.read_len, P.win_len, -1);
+            add_limits(S.L1, P.read_len, P.win_len, P.win_len <= 30 ? -1 : 30);
+            add_limits(S.L2, P.read_len, P.win_len, -1);
         } else {
-            add_limits(L1, P.read_len, P.win_len, P.band_half);
+            add_limits(S.L1, P.read_len, P.win_len, P.band_half);
         }
+        S.arena_end = std::max({S.arena_end, P.read_pos + P.read_len, P.win_pos + P.win_len});
     }
-    return ESP_OK;
+}
+
+static void merge(ScanOut &into, const ScanOut &s) {
+    into.L1.tb_words = std::max(into.L1.tb_words, s.L1.tb_words);
+    into.L1.rb_words = std::max(into.L1.rb_words, s.L1.rb_words);
+    into.L1.max_m = std::max(into.L1.max_m, s.L1.max_m);
+    into.L2.tb_words = std::max(into.L2.tb_words, s.L2.tb_words);
+    into.L2.rb_words = std::max(into.L2.rb_words, s.L2.rb_words);
+    into.L2.max_m = std::max(into.L2.max_m, s.L2.max_m);
+    into.arena_end = std::max(into.arena_end, s.arena_end);
+}
+
+// Per-chunk scans (chunk c = pairs [bounds[c], bounds[c+1])), in parallel.
+static void scan_chunks(int mode, const esp_pair *pairs, const std::vector<uint64_t> &bounds,
+                        std::vector<ScanOut> &out) {
+    const size_t C = bounds.size() - 1;
+    out.assign(C, ScanOut{});
+    const uint64_t n = bounds.back();
+    unsigned T = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (n < (1u << 16)) T = 1;
+    // split every chunk into T slices; each worker scans slice t of every chunk
+    std::vector<std::vector<ScanOut>> part(T, std::vector<ScanOut>(C));
+    auto work = [&](unsigned t) {
+        for (size_t c = 0; c < C; c++) {
+            uint64_t a = bounds[c], b = bounds[c + 1], len = b - a;
+            scan_range(mode, pairs, a + len * t / T, a + len * (t + 1) / T, part[t][c]);
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < T; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th) x.join();
+    for (unsigned t = 0; t < T; t++)
+        for (size_t c = 0; c < C; c++) merge(out[c], part[t][c]);
 }
 
 int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
@@ -426,8 +470,16 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
     CK(h, cudaSetDevice(h->device));
-    Limits L1, L2;
-    batch_common(h, mode, pairs, n_pairs, L1, L2);
+    // Large batches run as a pipeline of chunks: the inputs of chunk c+1 and
+    // the results of chunk c-1 cross the host link while chunk c computes.
+    const uint64_t C = n_pairs >= (1u << 20) ? 4 : 1;
+    std::vector<uint64_t> bounds(C + 1);
+    for (uint64_t c = 0; c <= C; c++) bounds[c] = n_pairs * c / C;
+    std::vector<ScanOut> sc;
+    scan_chunks(mode, pairs, bounds, sc);
+    ScanOut all;
+    for (auto &s : sc) merge(all, s);
+    const Limits &L1 = all.L1, &L2 = all.L2;
     if (L1.max_m > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     size_t sz_pairs = (n_pairs * sizeof(esp_pair) + 255) / 256 * 256;
     size_t sz_iv = (n_iv_count * sizeof(esp_n_interval) + 255) / 256 * 256;
@@ -444,18 +496,61 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     esp_extension *dout = (esp_extension *)(da + sz_arena);
     uint32_t *dcig = (uint32_t *)((uint8_t *)dout + sz_out);
     cudaStream_t st = h->stream;
-    CK(h, cudaMemcpyAsync(dp, pairs, n_pairs * sizeof(esp_pair), cudaMemcpyHostToDevice, st));
+    if (C == 1) {
+        CK(h, cudaMemcpyAsync(dp, pairs, n_pairs * sizeof(esp_pair), cudaMemcpyHostToDevice, st));
+        if (n_iv_count)
+            CK(h, cudaMemcpyAsync(div, n_iv, n_iv_count * sizeof(esp_n_interval), cudaMemcpyHostToDevice, st));
+        CK(h, cudaMemcpyAsync(da, arena, arena_bytes, cudaMemcpyHostToDevice, st));
+        CK(h, cudaMemsetAsync(da + arena_bytes, 0, 16, st));
+        rc = enqueue_batch(h, mode, dp, n_pairs, da, arena_bytes, div, n_iv_count, K, L1, L2, dout,
+                           dcig, cigar_stride, st);
+        if (rc != ESP_OK) return rc;
+        CK(h, cudaMemcpyAsync(out, dout, n_pairs * sizeof(esp_extension), cudaMemcpyDeviceToHost, st));
+        if (cigar && cigar_stride)
+            CK(h, cudaMemcpyAsync(cigar, dcig, n_pairs * (size_t)cigar_stride * 4, cudaMemcpyDeviceToHost, st));
+        CK(h, cudaStreamSynchronize(st));
+        return ESP_OK;
+    }
+    if (!h->copy_stream) CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    cudaStream_t cs = h->copy_stream;
+    std::vector<cudaEvent_t> ev(2 * C);
+    for (auto &e : ev) CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // inputs, chunk by chunk: the pairs and the arena prefix the chunk reads
+    // (the last chunk also gets the zero tail that 64-bit code loads read)
     if (n_iv_count)
-        CK(h, cudaMemcpyAsync(div, n_iv, n_iv_count * sizeof(esp_n_interval), cudaMemcpyHostToDevice, st));
-    CK(h, cudaMemcpyAsync(da, arena, arena_bytes, cudaMemcpyHostToDevice, st));
-    CK(h, cudaMemsetAsync(da + arena_bytes, 0, 16, st));
-    rc = enqueue_batch(h, mode, dp, n_pairs, da, arena_bytes, div, n_iv_count, K, L1, L2, dout,
-                       dcig, cigar_stride, st);
-    if (rc != ESP_OK) return rc;
-    CK(h, cudaMemcpyAsync(out, dout, n_pairs * sizeof(esp_extension), cudaMemcpyDeviceToHost, st));
-    if (cigar && cigar_stride)
-        CK(h, cudaMemcpyAsync(cigar, dcig, n_pairs * (size_t)cigar_stride * 4, cudaMemcpyDeviceToHost, st));
+        CK(h, cudaMemcpyAsync(div, n_iv, n_iv_count * sizeof(esp_n_interval), cudaMemcpyHostToDevice, cs));
+    uint64_t copied = 0;  // arena bytes already sent
+    for (uint64_t c = 0; c < C; c++) {
+        const uint64_t a = bounds[c], n = bounds[c + 1] - a;
+        CK(h, cudaMemcpyAsync(dp + a, pairs + a, n * sizeof(esp_pair), cudaMemcpyHostToDevice, cs));
+        uint64_t need = c + 1 == C ? arena_bytes
+                                   : std::min<uint64_t>(arena_bytes, (sc[c].arena_end + 3) / 4 + 16);
+        if (need > copied) {
+            CK(h, cudaMemcpyAsync(da + copied, arena + copied, need - copied, cudaMemcpyHostToDevice, cs));
+            copied = need;
+        }
+        if (c + 1 == C) CK(h, cudaMemsetAsync(da + arena_bytes, 0, 16, cs));
+        CK(h, cudaEventRecord(ev[c], cs));
+    }
+    for (uint64_t c = 0; c < C; c++) {
+        const uint64_t a = bounds[c], n = bounds[c + 1] - a;
+        CK(h, cudaStreamWaitEvent(st, ev[c], 0));
+        rc = enqueue_batch(h, mode, dp + a, n, da, arena_bytes, div, n_iv_count, K, L1, L2,
+                           dout + a, dcig + a * cigar_stride, cigar_stride, st);
+        if (rc != ESP_OK) {
+            for (auto &e : ev) cudaEventDestroy(e);
+            return rc;
+        }
+        CK(h, cudaEventRecord(ev[C + c], st));
+        CK(h, cudaStreamWaitEvent(cs, ev[C + c], 0));
+        CK(h, cudaMemcpyAsync(out + a, dout + a, n * sizeof(esp_extension), cudaMemcpyDeviceToHost, cs));
+        if (cigar && cigar_stride)
+            CK(h, cudaMemcpyAsync(cigar + a * cigar_stride, dcig + a * cigar_stride,
+                                  n * (size_t)cigar_stride * 4, cudaMemcpyDeviceToHost, cs));
+    }
+    CK(h, cudaStreamSynchronize(cs));
     CK(h, cudaStreamSynchronize(st));
+    for (auto &e : ev) cudaEventDestroy(e);
     return ESP_OK;
 }
 

@@ -2,6 +2,9 @@
 // myers_ea::* and engine::myers::*, and the batch API.
 #include <cuda_runtime.h>
 
+#include <thread>
+#include <vector>
+
 #include "esp_host.h"
 
 namespace {
@@ -171,12 +174,26 @@ int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
                          const esp_n_interval *n_iv, uint64_t n_iv_count,
                          esp_myers_result *out) {
     if (!h || !out || (n_pairs && (!pairs || !arena))) return fail(h, ESP_EINVAL, "null argument");
+    // longest read (sizes the kernel's limb count); large batches are
+    // scanned by several host threads
     uint32_t mx = 1;
-    for (uint64_t k = 0; k < n_pairs; k++) {
-        if (pairs[k].read_len > (uint32_t)LONG_MAX_M)
-            return fail(h, ESP_EINVAL, "Myers read length must be <= 256");
-        mx = std::max(mx, pairs[k].read_len);
+    {
+        unsigned T = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        if (n_pairs < (1u << 16)) T = 1;
+        std::vector<uint32_t> part(T, 1);
+        auto work = [&](unsigned t) {
+            uint32_t m = 1;
+            for (uint64_t k = n_pairs * t / T, e = n_pairs * (t + 1) / T; k < e; k++)
+                m = std::max(m, pairs[k].read_len);
+            part[t] = m;
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < T; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+        for (uint32_t m : part) mx = std::max(mx, m);
     }
+    if (mx > (uint32_t)LONG_MAX_M) return fail(h, ESP_EINVAL, "Myers read length must be <= 256");
     CK(h, cudaSetDevice(h->device));
     size_t sz_p = (n_pairs * sizeof(esp_myers_pair) + 255) / 256 * 256;
     size_t sz_iv = (n_iv_count * sizeof(esp_n_interval) + 255) / 256 * 256;

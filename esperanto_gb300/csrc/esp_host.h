@@ -17,6 +17,7 @@ struct esp_handle {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host-batch pipelining (created on first use)
     std::string err;
     uint64_t launches = 0;
     int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
