@@ -1,6 +1,6 @@
 """Benchmark of the GB300 alignment inner loop (one JSON line on rank 0).
 
-Default workload (config 2) = the mixed-length batched configuration:
+Default workload = the mixed-length batch:
 4,194,304 read x window pairs, read length U[50,300], band half-width in
 {16,32,64,128} w.p. {.4,.3,.2,.1}, windows of read + 2*half, banded affine DP
 with full CIGAR traceback, in one persistent length-binned launch.  Other
@@ -43,8 +43,9 @@ OPS_PER_CELL = 18
 # Myers: 10 32-bit logic/add/shift ops per 32-cell limb per text column.
 MYERS_OPS_PER_CELL = 10.0 / 32.0
 # ncu DRAM bytes (read + write) of the DP kernel per launch, from the
-# committed summaries: config 0 (65,536 pairs, one launch) and config 1
-# (1,048,576 Myers pairs, one launch); config 2 per DP cell, captured on a
+# committed summaries: the 150 x 214 banded batch (65,536 pairs, one launch)
+# and the Myers batch (1,048,576 pairs, one launch); the mixed-length batch
+# per DP cell, captured on a
 # 524,288-pair case of the same distribution and scaled by cells.
 TRAFFIC_BYTES = {0: 50.3e6 + 348.3e6, 1: 125.5e6 + 9.3e6}
 TRAFFIC_PER_CELL = {2: (2713001472 + 6431804160) / 7716062109}
@@ -138,7 +139,8 @@ class Workload:
 
 
 class GotohWorkload(Workload):
-    """Configs 0 and 2: run_band with traceback over a pair batch."""
+    """The banded Gotoh batches (150 x 214 pairs; the mixed-length batch):
+    run_band with traceback over a pair batch."""
 
     def __init__(self, config):
         self.config = config
@@ -390,7 +392,7 @@ class SpliceWorkload(Workload):
 
 
 def serve_bench(args):
-    """Config 4: the serving loop on a 3.1-Gbp resident genome.  Measures the
+    """The serving workload: the serving loop on a 3.1-Gbp resident genome.  Measures the
     saturated throughput (closed loop), then Poisson arrivals of 1k-64k-read
     requests (log-uniform) at 70% and 80% of it, reporting p50/p99 latency."""
     import torch

@@ -112,7 +112,8 @@ def decode_pair(arena: np.ndarray, pair, n_iv: Optional[np.ndarray] = None) -> T
 
 
 def synth_gotoh(seed: int, n_pairs: int, config: int):
-    """Seeded Gotoh workload (config 0 or 2): (arena, pairs)."""
+    """Seeded Gotoh workload, shape 0 (150 x 214 banded) or 2 (mixed length):
+    (arena, pairs)."""
     L = N.lib()
     L.esp_synth_gotoh_size.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64)]
     L.esp_synth_gotoh.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p, C.c_uint64,
@@ -190,7 +191,7 @@ def cigar_of(cig_row: np.ndarray, n_ops: int):
 
 
 def synth_myers(seed: int, n_pairs: int):
-    """Seeded Myers workload (config 1): (arena, myers pairs)."""
+    """Seeded Myers workload (150-bp queries vs 200-bp texts): (arena, myers pairs)."""
     L = N.lib()
     nb = C.c_uint64()
     rc = L.esp_synth_myers_size(seed, n_pairs, C.byref(nb))

@@ -77,11 +77,11 @@ struct Shape {
     uint32_t L, n, half;
 };
 
-// Config 0: 150-bp reads from a 214-bp window at offset 32, band half 32.
-// Config 2: L ~ U[50,300], half from {16,32,64,128} w.p. {.4,.3,.2,.1},
+// Shape 0 (banded batch): 150-bp reads from a 214-bp window at offset 32, band half 32.
+// Shape 2 (mixed-length batch): L ~ U[50,300], half from {16,32,64,128} w.p. {.4,.3,.2,.1},
 //           window L + 2*half, read drawn at offset `half`.
-Shape shape_of(int config, Rng &rng) {
-    if (config == 0) return {150, 214, 32};
+Shape shape_of(int shape, Rng &rng) {
+    if (shape == 0) return {150, 214, 32};
     uint32_t L = 50 + rng.below(251);
     double u = rng.unit();
     uint32_t h = u < 0.4 ? 16 : (u < 0.7 ? 32 : (u < 0.9 ? 64 : 128));
@@ -106,13 +106,13 @@ void parallel_for(uint64_t n, F f) {
 extern "C" {
 
 // Sizes of a Gotoh workload: total arena bytes (including 16 bytes of
-// padding) for `n_pairs` pairs of configuration 0 or 2.
-int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int config, uint64_t *arena_bytes) {
-    if (!arena_bytes || (config != 0 && config != 2)) return ESP_EINVAL;
+// padding) for `n_pairs` pairs of shape 0 or 2.
+int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int shape, uint64_t *arena_bytes) {
+    if (!arena_bytes || (shape != 0 && shape != 2)) return ESP_EINVAL;
     std::vector<uint64_t> bases(n_pairs);
     parallel_for(n_pairs, [&](uint64_t i) {
         Rng r(pair_seed(seed, i));
-        Shape s = shape_of(config, r);
+        Shape s = shape_of(shape, r);
         bases[i] = s.L + s.n;
     });
     uint64_t tot = 0;
@@ -122,14 +122,14 @@ int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int config, uint64_t *
 }
 
 // Fill a Gotoh workload: pairs[i] gets the read and window of pair i packed
-// into `arena` (zeroed by this call), band offset/half of the configuration.
-int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
+// into `arena` (zeroed by this call), band offset/half of the shape.
+int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int shape, uint8_t *arena,
                     uint64_t arena_bytes, esp_pair *pairs) {
-    if (!arena || !pairs || (config != 0 && config != 2)) return ESP_EINVAL;
+    if (!arena || !pairs || (shape != 0 && shape != 2)) return ESP_EINVAL;
     std::vector<Shape> shp(n_pairs);
     parallel_for(n_pairs, [&](uint64_t i) {
         Rng r(pair_seed(seed, i));
-        shp[i] = shape_of(config, r);
+        shp[i] = shape_of(shape, r);
     });
     std::vector<uint64_t> pos(n_pairs + 1, 0);
     for (uint64_t i = 0; i < n_pairs; i++) pos[i + 1] = pos[i] + shp[i].L + shp[i].n;
@@ -149,7 +149,7 @@ int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
             uint64_t first_byte = pos[lo] >> 2, last_byte = pos[hi] >> 2;
             for (uint64_t i = lo; i < hi; i++) {
                 Rng r(pair_seed(seed, i));
-                Shape s = shape_of(config, r);  // same draws as the sizing pass
+                Shape s = shape_of(shape, r);  // same draws as the sizing pass
                 win.resize(s.n);
                 rd.resize(s.L);
                 for (uint32_t k = 0; k < s.n; k++) win[k] = r.base();
@@ -185,7 +185,7 @@ int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
     return ESP_OK;
 }
 
-// Config 1 (Myers): 200-bp uniform text; 90% of queries are 150 bases
+// Myers workload: 200-bp uniform text; 90% of queries are 150 bases
 // sampled from the text at a uniform start in [0, 50] with U{0..8} edits
 // (substitution / insertion / deletion, equally likely, at uniform read
 // positions), 10% are unrelated random sequence.
@@ -254,7 +254,7 @@ int esp_synth_myers(uint64_t seed, uint64_t n_pairs, uint8_t *arena, uint64_t ar
     return ESP_OK;
 }
 
-// Config 3 (splice): one contig per read.  Draw order per read (shared by
+// Splice workload: one contig per read.  Draw order per read (shared by
 // the sizing and filling passes): intron length, breakpoint, tail jitter,
 // decoy donors, decoy acceptors, supports, then sequence.
 struct SpliceShape {
@@ -387,7 +387,7 @@ int esp_synth_splice(uint64_t seed, uint64_t n_reads, uint8_t *genome_arena,
     return ESP_OK;
 }
 
-// Config 4 (serve): uniform-ACGT genome, equal contigs starting on whole
+// Serve workload: uniform-ACGT genome, equal contigs starting on whole
 // bytes; every 4 bases are one uniformly random byte.
 int esp_synth_genome(uint64_t seed, uint64_t total_bases, uint32_t n_contigs, uint8_t *arena,
                      uint64_t arena_bytes, esp_contig *contigs) {

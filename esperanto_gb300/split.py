@@ -328,7 +328,7 @@ def channel_a_batch(genome: Genome, reads: np.ndarray, read_arena: np.ndarray,
 
 
 def synth_splice(seed: int, n_reads: int):
-    """Seeded splice workload (config 3):
+    """Seeded splice workload (524,288-read rescue batch shape):
     (genome_arena, contigs, read_arena, reads, cands)."""
     L = N.lib()
     gb, rb, nc = C.c_uint64(), C.c_uint64(), C.c_uint64()

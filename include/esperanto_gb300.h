@@ -592,23 +592,23 @@ int esp_batch_run_band_noalloc(const esp_pair *pairs, uint64_t n_pairs, const ui
 /* ---- seeded synthetic workloads (the reference ships no datasets) ---- */
 
 /* Arena bytes (16 bytes of padding included) of a Gotoh workload:
- * config 0 = 150-bp reads vs 214-bp windows, band half 32 at offset 32;
- * config 2 = read length U[50,300], half in {16,32,64,128} w.p.
+ * shape 0 = 150-bp reads vs 214-bp windows, band half 32 at offset 32;
+ * shape 2 = read length U[50,300], half in {16,32,64,128} w.p.
  * {.4,.3,.2,.1}, window read + 2*half, offset half.  Error model: 1%
  * substitutions, 0.1% indels of length 1-3, A->G at 5% of A (T->C on
  * reverse-strand pairs). */
-int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int config, uint64_t *arena_bytes);
+int esp_synth_gotoh_size(uint64_t seed, uint64_t n_pairs, int shape, uint64_t *arena_bytes);
 /* Fill the workload into caller memory (host). */
-int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int config, uint8_t *arena,
+int esp_synth_gotoh(uint64_t seed, uint64_t n_pairs, int shape, uint8_t *arena,
                     uint64_t arena_bytes, esp_pair *pairs);
 
 /* Myers workload: 150-bp queries sampled from 200-bp uniform texts with
- * U{0..8} edits, 10% unrelated random queries (config 1). */
+ * U{0..8} edits, 10% unrelated random queries. */
 int esp_synth_myers_size(uint64_t seed, uint64_t n_pairs, uint64_t *arena_bytes);
 int esp_synth_myers(uint64_t seed, uint64_t n_pairs, uint8_t *arena, uint64_t arena_bytes,
                     esp_myers_pair *pairs);
 
-/* Splice workload (config 3): per read a contig exon1(300) + intron
+/* Splice workload: per read a contig exon1(300) + intron
  * (log-uniform 60..50,000, GT..AG planted) + exon2(300); the read is 150 bp
  * across the junction split at U[20,130] with the Gotoh error model;
  * candidates = the true junction plus decoys at every other GT within +-20
@@ -621,7 +621,7 @@ int esp_synth_splice(uint64_t seed, uint64_t n_reads, uint8_t *genome_arena,
                      uint64_t read_bytes, esp_splice_read *reads, esp_splice_cand *cands,
                      uint64_t n_cands);
 
-/* Serve workload (config 4): a uniform-ACGT genome of `total_bases` in
+/* Serve workload: a uniform-ACGT genome of `total_bases` in
  * `n_contigs` equal contigs (contig c starts at base c * stride, stride a
  * multiple of 4), and request reads: 2x150 paired-end fragments (insert
  * 250-450) at uniform coordinates with the Gotoh error model; each read's

@@ -1,4 +1,4 @@
-"""Shared GPU-vs-oracle comparison helpers (the oracle is the checker)."""
+"""Shared GPU-vs-oracle comparison helpers."""
 import functools
 
 import numpy as np
