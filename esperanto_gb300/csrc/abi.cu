@@ -13,10 +13,6 @@
 
 #include "esp_host.h"
 
-namespace {
-
-}  // namespace
-
 // Enqueue the DP launches of one batch whose inputs are on the device.
 int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_pairs,
                   const uint8_t *d_arena, uint64_t arena_bytes, const esp_n_interval *d_iv,
