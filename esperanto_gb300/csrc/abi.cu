@@ -60,7 +60,6 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         job.esc_list = h->d_esc;
         job.esc_count = h->d_ctr + 4;
         job.mode = mode == ESP_MODE_HINT ? 1 : 0;
-        job.max_m = (int)L1.max_m;
         CK(h, esp::launch_gotoh_warp(job, K, (int)warps, st));
         h->launches++;
         if (mode == ESP_MODE_HINT) {
@@ -148,7 +147,6 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     job.esc_list = h->d_esc;
     job.esc_count = h->d_ctr + 4;
     job.mode = mode == ESP_MODE_HINT ? 1 : 0;
-    job.max_m = (int)L1.max_m;
     if (per_class && h->autotune_ms) {
         // time every variant on every length class (best of two runs each);
         // the batch's results are those of the last run of each class
@@ -190,7 +188,6 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     if (mode == ESP_MODE_HINT) {
         esp::GotohJob j2 = job;
         j2.mode = 2;
-        j2.list_count = nullptr;
         j2.list = h->d_esc;
         j2.list_count = h->d_ctr + 4;
         j2.queue = h->d_ctr + 2;

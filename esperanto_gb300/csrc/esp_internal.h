@@ -54,7 +54,6 @@ struct GotohJob {
     uint32_t *rb;               // row-buffer scratch: slots * rb_words * 32 words
     uint64_t rb_words;
     uint32_t *queue;            // device work counter (zeroed before launch)
-    int max_m;                  // largest read length in the job
 };
 
 // Launch the persistent DP kernel with `warps` warps total.

@@ -119,7 +119,6 @@ extern "C" int esp_batch_run_band_noalloc(const esp_pair *pairs, uint64_t n_pair
     job.tb_words = tbw;
     job.rb = job.tb + warps * 32 * tbw;
     job.rb_words = rbw;
-    job.max_m = (int)limits->max_read_len;
     if (esp::launch_gotoh(job, K, (int)warps, 128, st, 1) != cudaSuccess) return ESP_ECUDA;
     return ESP_OK;
 }
