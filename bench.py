@@ -613,6 +613,9 @@ def main():
         "bad_status": bad,
         "gpu_launches": launches,
         "roofline": {"bound": "int_alu", "achieved": achieved_ops / 1e12,
+                     "hbm_achieved_gbs": (traffic / (ms / 1e3) / 1e9) if traffic else None,
+                     "hbm_frac": (traffic / (ms / 1e3) / 1e9 / peaks["hbm_gbs"])
+                     if traffic and peaks.get("hbm_gbs") else None,
                      "peak": peak_ops / 1e12, "unit": "Tops/s",
                      "frac": achieved_ops / peak_ops, "traffic": traffic,
                      "traffic_source": TRAFFIC_SOURCE.get(config),
