@@ -174,15 +174,17 @@ class GotohWorkload(Workload):
         if n > 2048 and not getattr(self, "no_autotune", False):
             # pick the DP variant per length class on this batch (untimed);
             # timed steps then replay one captured graph of the tuned launches
-            variants, ms = (C.c_int * 4)(), (C.c_double * 8)()
+            nv = 4  # kernel variants timed per class
+            variants, ms = (C.c_int * 4)(), (C.c_double * (5 * nv))()
             buf.check(L.esp_batch_autotune(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
                                            d_arena.data_ptr(), arena.nbytes, None, 0,
                                            C.byref(lim), C.byref(p), d_out.data_ptr(),
                                            d_cig.data_ptr(), self.stride, None, variants, ms))
-            self.autotune = {"classes": ["w>=196", "100<=w<196", "52<=w<100", "w<52"],
+            self.autotune = {"classes": ["w>=196", "100<=w<196", "52<=w<100", "w<52",
+                                         "whole list"],
                              "variants": list(variants),
-                             "ms": [[round(ms[2 * s], 3), round(ms[2 * s + 1], 3)]
-                                    for s in range(4)]}
+                             "ms": [[round(ms[nv * s + v], 3) for v in range(nv)]
+                                    for s in range(5)]}
 
         def step():
             buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,

@@ -166,6 +166,7 @@ def lib():
                                     C.POINTER(vp)]
     L.esp_genome_destroy.argtypes = [vp]
     L.esp_set_warp_max.argtypes = [vp, C.c_long]
+    L.esp_set_kernel_variant.argtypes = [vp, C.c_int]
     L.esp_batch_spliced_host.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, vp,
                                          C.c_uint64, vp, C.c_uint64, C.POINTER(ExtendParamsC),
                                          vp, vp, vp, C.c_uint32]

@@ -13,6 +13,26 @@
 
 #include "esp_host.h"
 
+// Kernel variant of a handle that was neither set nor tuned: the
+// ESP_GOTOH_VARIANT environment variable (0..3), else 1.
+static int default_variant() {
+    const char *v = getenv("ESP_GOTOH_VARIANT");
+    if (v && v[0] >= '0' && v[0] < '0' + esp::kGotohVariants && !v[1]) return v[0] - '0';
+    return 1;
+}
+
+// Whether band-mode batches of this handle run a paired kernel (set, or
+// chosen by autotuning for any length class).
+static bool band_paired(esp_handle *h, int mode) {
+    if (mode != ESP_MODE_BAND || !h->binning) return false;
+    if (h->tuned) {
+        for (int s = 0; s < esp::kLengthClasses; s++)
+            if (esp::gotoh_paired(h->tune[s])) return true;
+        return false;
+    }
+    return esp::gotoh_paired(h->variant < 0 ? default_variant() : h->variant);
+}
+
 // Enqueue the DP launches of one batch whose inputs are on the device.
 int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_pairs,
                   const uint8_t *d_arena, uint64_t arena_bytes, const esp_n_interval *d_iv,
@@ -77,21 +97,24 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
     uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
     uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    if (h->variant < 0) {
-        const char *v = getenv("ESP_GOTOH_VARIANT");
-        h->variant = (v && *v == '0') ? 0 : 1;
-    }
-    int var = h->variant;
+    if (h->variant < 0) h->variant = default_variant();
+    // the paired kernels need neighbours of the binned list with one band
+    // geometry: band mode only (hint offsets differ per pair)
+    auto usable = [&](int v) {
+        return esp::gotoh_paired(v) && (mode != ESP_MODE_BAND || !h->binning) ? v - 2 : v;
+    };
+    int var = usable(h->variant);
     // autotuned handle: one variant for every class runs as a single launch
     bool tuned_split = false;
-    if (h->tuned) {
+    if (h->tuned && mode == ESP_MODE_BAND) {
         for (int s = 1; s < esp::kLengthClasses; s++) tuned_split |= h->tune[s] != h->tune[0];
-        if (!tuned_split && h->tune[0] >= 0) var = h->tune[0];
+        if (!tuned_split && h->tune[0] >= 0) var = usable(h->tune[0]);
     }
     // the binned list runs per length class when the handle is autotuned (or
     // is being tuned); scratch then covers the widest variant in use
     const bool per_class = (tuned_split || h->autotune_ms) && h->binning && n_pairs > 32;
     int max_bps = 0;
+    bool paired = false;
     for (int v = 0; v < esp::kGotohVariants; v++) {
         bool used = v == var;
         if (per_class)
@@ -99,16 +122,18 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         if (!used) continue;
         if (h->gotoh_bps[v] == 0) h->gotoh_bps[v] = esp::gotoh_blocks_per_sm(128, v);
         max_bps = std::max(max_bps, h->gotoh_bps[v]);
+        paired |= esp::gotoh_paired(v);
     }
+    const uint64_t slot_pairs = paired ? 2 : 1;  // scratch slots per lane
     uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * max_bps * 4);
     uint64_t need_warps = (n_pairs + 31) / 32;
     uint64_t warps = std::min(want, need_warps);
-    uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes);
+    uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / (per_warp_bytes * slot_pairs));
     warps = std::min(warps, budget_warps);
     warps = (warps + 3) / 4 * 4;  // whole 128-thread blocks: every launched warp owns a slot
-    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * tbw * 32 * 4)) != ESP_OK)
+    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * slot_pairs * tbw * 32 * 4)) != ESP_OK)
         return rc;
-    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * rbw * 32 * 4)) != ESP_OK)
+    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * slot_pairs * rbw * 32 * 4)) != ESP_OK)
         return rc;
     if (mode == ESP_MODE_HINT &&
         (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
@@ -123,7 +148,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         CK(h, esp::launch_binning(d_pairs, n_pairs, mode == ESP_MODE_HINT ? 1 : 0, h->d_hist,
                                   h->d_order, h->num_sms, st,
                                   per_class ? h->d_ctr + 24 : nullptr));
-        h->launches += per_class ? 4 : 3;
+        h->launches += per_class ? 6 : 5;
         order = h->d_order;
     }
     esp::GotohJob job{};
@@ -148,19 +173,22 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     job.esc_count = h->d_ctr + 4;
     job.mode = mode == ESP_MODE_HINT ? 1 : 0;
     if (per_class && h->autotune_ms) {
-        // time every variant on every length class (best of two runs each);
-        // the batch's results are those of the last run of each class
+        // time every variant on every length class and, as row
+        // kLengthClasses, on the whole list in one launch (best of two runs
+        // each); the batch's results are those of the last run
         cudaEvent_t ev[2];
         CK(h, cudaEventCreate(&ev[0]));
         CK(h, cudaEventCreate(&ev[1]));
-        for (int s = 0; s < esp::kLengthClasses; s++)
+        for (int s = 0; s <= esp::kLengthClasses; s++)
             for (int v = 0; v < esp::kGotohVariants; v++) {
                 double best = 1e30;
                 for (int rep = 0; rep < 2; rep++) {
                     esp::GotohJob js = job;
-                    js.range = h->d_ctr + 24 + s;
-                    js.queue = h->d_ctr + 8 + 2 * s;
-                    CK(h, cudaMemsetAsync(h->d_ctr + 8 + 2 * s, 0, 8, st));
+                    if (s < esp::kLengthClasses) {
+                        js.range = h->d_ctr + 24 + s;
+                        js.queue = h->d_ctr + 8 + 2 * s;
+                    }
+                    CK(h, cudaMemsetAsync(js.queue, 0, 8, st));
                     CK(h, cudaEventRecord(ev[0], st));
                     CK(h, esp::launch_gotoh(js, K, (int)warps, 128, st, v));
                     CK(h, cudaEventRecord(ev[1], st));
@@ -205,19 +233,19 @@ int reserve_dp(esp_handle *h, uint64_t max_pairs, uint32_t max_m, uint32_t max_n
     add_limits(L2, max_m, max_n, -1);
     uint64_t tbw = std::max(L1.tb_words, L2.tb_words), rbw = std::max(L1.rb_words, L2.rb_words);
     uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    if (h->variant < 0) {
-        const char *v = getenv("ESP_GOTOH_VARIANT");
-        h->variant = (v && *v == '0') ? 0 : 1;
-    }
+    if (h->variant < 0) h->variant = default_variant();
     if (h->gotoh_bps[h->variant] == 0)
         h->gotoh_bps[h->variant] = esp::gotoh_blocks_per_sm(128, h->variant);
+    const uint64_t slot_pairs = esp::gotoh_paired(h->variant) ? 2 : 1;
     uint64_t warps = std::min<uint64_t>((uint64_t)h->num_sms * h->gotoh_bps[h->variant] * 4,
                                         (max_pairs + 31) / 32);
-    warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes));
+    warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / (per_warp_bytes * slot_pairs)));
     warps = (warps + 3) / 4 * 4;
     int rc;
-    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * tbw * 32 * 4)) != ESP_OK) return rc;
-    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * rbw * 32 * 4)) != ESP_OK) return rc;
+    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * slot_pairs * tbw * 32 * 4)) != ESP_OK)
+        return rc;
+    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * slot_pairs * rbw * 32 * 4)) != ESP_OK)
+        return rc;
     if ((rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, max_pairs * 4)) != ESP_OK) return rc;
     if ((rc = grow_device(h, (void **)&h->d_hist, &h->d_hist_cap, esp::bin_scratch_bytes())) != ESP_OK)
         return rc;
@@ -247,6 +275,14 @@ int esp_create(esp_handle **out, int device) {
 int esp_set_warp_max(esp_handle *h, long warp_max) {
     if (!h || warp_max < 0) return ESP_EINVAL;
     h->warp_max = warp_max;
+    return ESP_OK;
+}
+
+int esp_set_kernel_variant(esp_handle *h, int variant) {
+    if (!h || variant < -1 || variant >= esp::kGotohVariants) return ESP_EINVAL;
+    h->variant = variant;
+    h->tuned = false;
+    for (int s = 0; s < esp::kLengthClasses; s++) h->tune[s] = -1;
     return ESP_OK;
 }
 
@@ -465,7 +501,11 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     CK(h, cudaSetDevice(h->device));
     // Large batches run as a pipeline of chunks: the inputs of chunk c+1 and
     // the results of chunk c-1 cross the host link while chunk c computes.
-    const uint64_t C = n_pairs >= (1u << 20) ? 4 : 1;
+    // Not for the paired kernels: an item holds two pairs, so the longest
+    // items of a chunk outlast the chunk's other work (measured on the mixed
+    // workload: 1M pairs at 21.3 ms paired vs 17.9 ms one per thread, 4M at
+    // 64.4 vs 71.5) and the chunk tails cost more than the copies they hide.
+    const uint64_t C = n_pairs >= (1u << 20) && !band_paired(h, mode) ? 4 : 1;
     std::vector<uint64_t> bounds(C + 1);
     for (uint64_t c = 0; c <= C; c++) bounds[c] = n_pairs * c / C;
     std::vector<ScanOut> sc;
@@ -643,7 +683,7 @@ int esp_batch_autotune(esp_handle *h, int mode, const esp_pair *pairs, uint64_t 
     if (mode != ESP_MODE_BAND) return fail(h, ESP_EINVAL, "autotuning runs band-mode batches");
     if (n_pairs <= (uint64_t)std::max<long>(32, h->warp_max < 0 ? 2048 : h->warp_max))
         return fail(h, ESP_EINVAL, "autotuning needs a batch of the persistent kernel's size");
-    double t[esp::kLengthClasses * esp::kGotohVariants];
+    double t[(esp::kLengthClasses + 1) * esp::kGotohVariants];
     h->tuned = false;
     h->autotune_ms = t;
     int rc = esp_batch_extend_device(h, mode, pairs, n_pairs, arena, arena_bytes, n_iv,
@@ -652,12 +692,22 @@ int esp_batch_autotune(esp_handle *h, int mode, const esp_pair *pairs, uint64_t 
     if (rc != ESP_OK) return rc;
     cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
     CK(h, cudaStreamSynchronize(st));
-    for (int s = 0; s < esp::kLengthClasses; s++) {
-        int best = 0;
+    // per-class launches each end in a tail of idle SMs: split only when the
+    // sum of the classes' best times beats the best single launch
+    auto best_of = [&](int row) {
+        int b = 0;
         for (int v = 1; v < esp::kGotohVariants; v++)
-            if (t[s * esp::kGotohVariants + v] < t[s * esp::kGotohVariants + best]) best = v;
-        h->tune[s] = best;
-        if (variants) variants[s] = best;
+            if (t[row * esp::kGotohVariants + v] < t[row * esp::kGotohVariants + b]) b = v;
+        return b;
+    };
+    double split = 0;
+    for (int s = 0; s < esp::kLengthClasses; s++)
+        split += t[s * esp::kGotohVariants + best_of(s)];
+    const int whole = best_of(esp::kLengthClasses);
+    const bool one = t[esp::kLengthClasses * esp::kGotohVariants + whole] <= split;
+    for (int s = 0; s < esp::kLengthClasses; s++) {
+        h->tune[s] = one ? whole : best_of(s);
+        if (variants) variants[s] = h->tune[s];
     }
     if (ms) memcpy(ms, t, sizeof(t));
     h->tuned = true;

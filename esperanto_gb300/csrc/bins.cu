@@ -1,11 +1,13 @@
 // bins.cu -- length-binned work list for the persistent DP kernels.
 //
-// Pairs are counting-sorted on the device by a 16-bit geometry key (band
-// width bucket, read length bucket) in DESCENDING cost order, so that (a)
-// the 32 pairs a warp takes from the queue share their loop trip counts and
+// Pairs are counting-sorted on the device by a 20-bit geometry key (columns
+// per row, rows; both exact below 1023) in DESCENDING cost order, so that
+// (a) the 32 pairs a warp takes from the queue share their loop trip counts,
 // (b) the most expensive pairs start first (the tail of the launch is made
-// of cheap pairs).  Three small kernels: histogram, scan, scatter; warp-
-// aggregated atomics keep a single hot bin (uniform batches) cheap.
+// of cheap pairs) and (c) neighbours in the list usually have identical band
+// geometry, which the two-pairs-per-thread kernel needs.  Kernels:
+// histogram, a three-phase scan, scatter; warp-aggregated atomics keep a
+// single hot bin (uniform batches) cheap.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -14,10 +16,13 @@
 
 namespace esp {
 
-static constexpr int NBINS = 1 << 16;
+static constexpr int KEY_BITS = 10;
+static constexpr int NBINS = 1 << (2 * KEY_BITS);
+static constexpr int SCAN_TILE = 1024;  // counters per block of the scan
+static constexpr int SCAN_BLOCKS = NBINS / SCAN_TILE;
 
 // Key: larger = more expensive.  w = columns per row (band width or window),
-// m = rows.  Both bucketed to 8 bits.
+// m = rows.
 __device__ __forceinline__ uint32_t geometry_key(const esp_pair &P, int mode) {
     uint32_t m = P.read_len, n = P.win_len;
     uint32_t w;
@@ -29,9 +34,8 @@ __device__ __forceinline__ uint32_t geometry_key(const esp_pair &P, int mode) {
         uint64_t bw = 2ull * h + 1;
         w = (uint32_t)(bw < n ? bw : n);
     }
-    uint32_t wb = w >= 1020 ? 255 : (w >> 2);
-    uint32_t mb = m >= 2040 ? 255 : (m >> 3);
-    return (wb << 8) | mb;
+    const uint32_t top = (1u << KEY_BITS) - 1;
+    return ((w < top ? w : top) << KEY_BITS) | (m < top ? m : top);
 }
 
 __device__ __forceinline__ void agg_add(uint32_t *ctr, uint32_t key, uint32_t *slot) {
@@ -56,29 +60,67 @@ __global__ void bin_hist(const esp_pair *__restrict__ pairs, uint64_t n, int mod
     }
 }
 
-// Exclusive scan of NBINS counters by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) bin_scan(uint32_t *__restrict__ hist) {
-    __shared__ uint32_t part[1024];
-    const int per = NBINS / 1024;
-    uint32_t *h = hist + threadIdx.x * per;
-    uint32_t s = 0;
-#pragma unroll 1
-    for (int k = 0; k < per; k++) s += h[k];
-    part[threadIdx.x] = s;
+// Exclusive scan of the NBINS counters in three phases: tile sums, a scan of
+// the tile sums (one block), tile scans offset by their prefix.  part[] holds
+// SCAN_BLOCKS words after the counters.
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_warp,
+                                                       uint32_t &total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    uint32_t wpre = 0;
+    total = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t w = s_warp[k];
+        if (k < wid) wpre += w;
+        total += w;
+    }
+    return wpre + x - v;
+}
+
+__global__ void __launch_bounds__(256) bin_scan_up(const uint32_t *__restrict__ hist,
+                                                   uint32_t *__restrict__ part) {
+    __shared__ uint32_t s_warp[8];
+    uint4 q = reinterpret_cast<const uint4 *>(hist + (size_t)blockIdx.x * SCAN_TILE)[threadIdx.x];
+    uint32_t total;
+    block_excl_scan256(q.x + q.y + q.z + q.w, s_warp, total);
+    if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) bin_scan_top(uint32_t *__restrict__ part) {
+    __shared__ uint32_t s[1024];
+    uint32_t v = threadIdx.x < SCAN_BLOCKS ? part[threadIdx.x] : 0;
+    s[threadIdx.x] = v;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+        uint32_t y = threadIdx.x >= (unsigned)off ? s[threadIdx.x - off] : 0;
         __syncthreads();
-        part[threadIdx.x] += v;
+        s[threadIdx.x] += y;
         __syncthreads();
     }
-    uint32_t run = part[threadIdx.x] - s;
-#pragma unroll 1
-    for (int k = 0; k < per; k++) {
-        uint32_t c = h[k];
-        h[k] = run;
-        run += c;
-    }
+    if (threadIdx.x < SCAN_BLOCKS) part[threadIdx.x] = s[threadIdx.x] - v;
+}
+
+__global__ void __launch_bounds__(256) bin_scan_down(uint32_t *__restrict__ hist,
+                                                     const uint32_t *__restrict__ part) {
+    __shared__ uint32_t s_warp[8];
+    uint4 *tile = reinterpret_cast<uint4 *>(hist + (size_t)blockIdx.x * SCAN_TILE);
+    uint4 q = tile[threadIdx.x];
+    uint32_t total;
+    uint32_t run = part[blockIdx.x] + block_excl_scan256(q.x + q.y + q.z + q.w, s_warp, total);
+    uint4 r;
+    r.x = run;
+    r.y = r.x + q.x;
+    r.z = r.y + q.y;
+    r.w = r.z + q.z;
+    tile[threadIdx.x] = r;
 }
 
 __global__ void bin_scatter(const esp_pair *__restrict__ pairs, uint64_t n, int mode,
@@ -137,7 +179,7 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
     return cudaGetLastError();
 }
 
-size_t bin_scratch_bytes() { return (size_t)NBINS * sizeof(uint32_t); }
+size_t bin_scratch_bytes() { return (size_t)(NBINS + SCAN_BLOCKS) * sizeof(uint32_t); }
 
 // Length classes of the binned list (descending cost): band/window width
 // w >= 196, [100, 196), [52, 100), < 52 columns.  bounds[s], bounds[s+1] is
@@ -145,9 +187,11 @@ size_t bin_scratch_bytes() { return (size_t)NBINS * sizeof(uint32_t); }
 __global__ void class_bounds(const uint32_t *__restrict__ hist, uint64_t n,
                              uint32_t *__restrict__ bounds) {
     if (threadIdx.x == 0) {
-        const uint32_t first_key[3] = {(48u << 8) | 255u, (24u << 8) | 255u, (12u << 8) | 255u};
+        const uint32_t top = (1u << KEY_BITS) - 1;
+        const uint32_t first_w[3] = {195u, 99u, 51u};  // widest width of classes 1..3
         bounds[0] = 0;
-        for (int s = 0; s < 3; s++) bounds[s + 1] = hist[NBINS - 1 - first_key[s]];
+        for (int s = 0; s < 3; s++)
+            bounds[s + 1] = hist[NBINS - 1 - ((first_w[s] << KEY_BITS) | top)];
         bounds[4] = (uint32_t)n;
     }
 }
@@ -160,7 +204,9 @@ cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t
     uint64_t need = (n + 255) / 256;
     if ((uint64_t)grid > need) grid = (int)(need ? need : 1);
     bin_hist<<<grid, 256, 0, st>>>(pairs, n, mode, hist);
-    bin_scan<<<1, 1024, 0, st>>>(hist);
+    bin_scan_up<<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
+    bin_scan_top<<<1, 1024, 0, st>>>(hist + NBINS);
+    bin_scan_down<<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
     if (bounds) class_bounds<<<1, 32, 0, st>>>(hist, n, bounds);
     bin_scatter<<<grid, 256, 0, st>>>(pairs, n, mode, hist, order);
     return cudaGetLastError();

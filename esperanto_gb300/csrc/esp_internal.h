@@ -57,10 +57,14 @@ struct GotohJob {
 };
 
 // Launch the persistent DP kernel with `warps` warps total.
-// variant 0: 3 resident 128-thread blocks per SM (168 registers); 1: 4 blocks.
+// variant 0: one pair per thread, 3 resident 128-thread blocks per SM (168
+// registers); 1: 4 blocks.  Variants 2 / 3: two pairs of identical geometry
+// per thread in 16x2 lanes (neighbours of the binned list), 3 / 4 blocks;
+// their scratch per warp is twice tb_words and twice rb_words per lane.
 cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, int block,
                          cudaStream_t st, int variant);
-constexpr int kGotohVariants = 2;
+constexpr int kGotohVariants = 4;
+constexpr bool gotoh_paired(int variant) { return variant >= 2; }
 
 // Warp-per-pair DP kernel (per-call drop-in, small batches): `warps` warps
 // stride over the pairs; each warp owns tb_words + rb_words words of the

@@ -937,6 +937,333 @@ cudaError_t launch_gotoh_warp(const GotohJob &job, const GotohConst &k, int warp
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Two pairs per thread in 16x2 SIMD lanes.  Two pairs with identical band
+// geometry and N-free windows share one thread: every register holds the
+// scaled key of pair A in its low half and of pair B in its high half, and
+// the half-word operations (add-max, 3-way max) evaluate both cells at once
+// with the arithmetic above (values stay inside int16: H <= 8191 by the
+// score-range rule, gap keys >= -16384 - 4*ext).  Substitution scores of
+// both cells come from one PRMT over the two rows' LUT words.  The traceback
+// words, row maxima and touches of each pair are exactly those of the
+// thread-per-pair kernel, and each pair's traceback is walked by the same
+// code (its words at stride 32, pair B's region after pair A's).
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t NEG2 = 0xC000C000u;   // E/F sentinel (-16384) in both halves
+constexpr uint32_t VNEG2 = 0x80008000u;  // -32768: max against it is a plain add
+constexpr uint32_t KEEP2 = 0xFFFCFFFCu;
+
+struct Strip2 {
+    uint32_t Hl[STRIP], Fl[STRIP], rmax[STRIP];
+    uint32_t la[STRIP], lb[STRIP];
+    uint32_t arg[STRIP];   // first column of the row maximum: pair A low half, B high
+    uint32_t lohi[STRIP];  // row window: first column low half, last column high half
+    uint32_t tright;       // bit r (A) / 8 + r (B): H at the row's last column is the max
+};
+
+__device__ __forceinline__ uint32_t prmt(uint32_t lo, uint32_t hi, uint32_t sel) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(lo), "r"(hi), "r"(sel));
+    return r;
+}
+
+// Row maximum and its first column for both lanes.  Hp and the running max
+// are in [0, 32766], so old + 0x8000 - Hp per half neither carries nor
+// borrows across halves and its bit 15 is set exactly when old >= Hp; PRMT's
+// sign-replicate mode spreads that bit into a keep mask per half.
+__device__ __forceinline__ void row_max2(uint32_t &rmax, uint32_t &arg, uint32_t Hp, uint32_t jj) {
+    uint32_t t = rmax + 0x80008000u - Hp;
+    uint32_t keep = prmt(t, 0u, 0xBB99u);
+    rmax = (rmax & keep) | (Hp & ~keep);
+    arg = (arg & keep) | (jj & ~keep);
+}
+
+template <int MASK>
+__device__ __forceinline__ void dp_column2(Strip2 &S, const uint32_t oe1, const uint32_t oe4,
+                                           const uint32_t ex4, int j, uint32_t sel, uint32_t &upH,
+                                           uint32_t &upE, uint32_t diag, uint32_t &wa,
+                                           uint32_t &wb) {
+    wa = 0;
+    wb = 0;
+    uint32_t d = diag;
+    const uint32_t jj = (uint32_t)j * 0x10001u;
+#pragma unroll
+    for (int r = 0; r < STRIP; r++) {
+        uint32_t left = S.Hl[r];
+        uint32_t kE = __viaddmax_s16x2(upE, ex4, __viaddmax_s16x2(upH, oe1, VNEG2));
+        uint32_t kF = __viaddmax_s16x2(S.Fl[r], ex4, __viaddmax_s16x2(left, oe4, VNEG2));
+        uint32_t E4 = kE & KEEP2;
+        uint32_t F4 = kF & KEEP2;
+        uint32_t kd = __viaddmax_s16x2(d, prmt(S.la[r], S.lb[r], sel), 0x00030003u);
+        uint32_t key = __vimax3_s16x2(kd, kE | 0x00010001u, F4);
+        uint32_t Hp = (key & KEEP2) | 0x00020002u;
+        wa = mad_u32(wa, 4u, key & 0x00030003u);
+        wb = mad_u32(wb, 4u, (kE & 0x00010001u) | (kF & 0x00020002u));
+        if (MASK) {
+            const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
+            if ((j >= lo) & (j <= hi)) {
+                row_max2(S.rmax[r], S.arg[r], Hp, jj);
+                if (j == hi) {  // the row's last column: is its H the row maximum?
+                    uint32_t eq = S.rmax[r] ^ Hp;
+                    if ((eq & 0xffffu) == 0) S.tright |= 1u << r;
+                    if ((eq >> 16) == 0) S.tright |= 0x100u << r;
+                }
+            } else {
+                Hp = 0x00020002u;
+                E4 = NEG2;
+                F4 = NEG2;
+            }
+        } else {
+            row_max2(S.rmax[r], S.arg[r], Hp, jj);
+        }
+        d = left;
+        S.Hl[r] = Hp;
+        S.Fl[r] = F4;
+        upH = Hp;
+        upE = E4;
+    }
+}
+
+// Columns [a, b] for both pairs; rb holds (H, E) of both pairs per column
+// (one uint2 per lane and column).
+template <int MASK, bool CHECK>
+__device__ __forceinline__ void dp_cols2(Strip2 &S, const uint32_t oe1, const uint32_t oe4,
+                                         const uint32_t ex4, int a, int b, uint32_t &diag,
+                                         const Seq &winA, const Seq &winB, uint2 *rb, int plo,
+                                         int phi, int lo7, uint32_t *tbA, uint32_t *tbB) {
+    uint2 *rbr = rb + (size_t)(a - plo) * 32;
+    uint2 wn0 = make_uint2(0u, 0u), wn1 = make_uint2(0u, 0u);
+    if (!CHECK) {  // interior: the row above two columns ahead
+        wn0 = rbr[0];
+        if (a + 1 <= b) wn1 = rbr[32];
+    }
+    for (int j = a; j <= b;) {
+        uint32_t cwA = load16(winA.arena, winA.pos + (uint64_t)(j - 1));
+        uint32_t cwB = load16(winB.arena, winB.pos + (uint64_t)(j - 1));
+        int cnt = min(16, b - j + 1);
+#pragma unroll 1
+        for (int k = 0; k < cnt; k++, j++) {
+            uint32_t sel = (cwA >> 30) * 0x11u + (cwB >> 30) * 0x1100u + 0xC480u;
+            cwA <<= 2;
+            cwB <<= 2;
+            uint2 w = make_uint2(0x00020002u, NEG2);
+            if (CHECK) {
+                if (j <= phi) w = *rbr;
+            } else {
+                w = wn0;
+                wn0 = wn1;
+                if (j + 2 <= b) wn1 = rbr[64];
+            }
+            uint32_t upH = w.x, upE = w.y;
+            uint32_t wa, wb;
+            dp_column2<MASK>(S, oe1, oe4, ex4, j, sel, upH, upE, diag, wa, wb);
+            diag = w.x;
+            uint2 packed = make_uint2(upH, upE);
+            if (CHECK) {
+                if (j >= lo7) rb[(size_t)(j - lo7) * 32] = packed;
+            } else {
+                rbr[(ptrdiff_t)(plo - lo7) * 32] = packed;
+            }
+            *tbA = __byte_perm(wa, wb, 0x5410);
+            *tbB = __byte_perm(wa, wb, 0x7632);
+            tbA += 32;
+            tbB += 32;
+            rbr += 32;
+        }
+    }
+}
+
+// Fill the DP of two pairs with identical geometry (shared g, m, n, sw).
+__device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut, int m, int n,
+                         const Geo &g, const Seq &readA, const Seq &readB, const Seq &winA,
+                         const Seq &winB, uint32_t *tbA, uint32_t *tbB, int sw, uint2 *rb,
+                         FillResult &FA, FillResult &FB) {
+    const uint32_t oe1 = (uint32_t)(K.oe1 & 0xffff) * 0x10001u;
+    const uint32_t oe4 = (uint32_t)(K.oe4 & 0xffff) * 0x10001u;
+    const uint32_t ex4 = (uint32_t)(K.ex4 & 0xffff) * 0x10001u;
+    FA.bestHp = FB.bestHp = 2;
+    FA.best_i = FA.best_j = FB.best_i = FB.best_j = 0;
+    FA.trow = FB.trow = 0;
+    FA.tleft = FA.tclamp = FB.tleft = FB.tclamp = false;
+    int nstrips = (m + STRIP - 1) / STRIP;
+    int plo = g.lo(1), phi = g.hi(min(STRIP, m));
+    for (int k = 0; k <= phi - plo; k++) rb[(size_t)k * 32] = make_uint2(0x00020002u, NEG2);
+    Strip2 S;
+    for (int s = 0; s < nstrips; s++) {
+        int i0 = s * STRIP + 1;
+        int nact = min(STRIP, m - i0 + 1);
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            S.lohi[r] = (uint32_t)g.lo(i0 + r) | ((uint32_t)g.hi(i0 + r) << 16);
+            S.Hl[r] = 0x00020002u;
+            S.Fl[r] = NEG2;
+            S.rmax[r] = 0u;
+            S.arg[r] = 0u;
+        }
+        S.tright = 0u;
+        int clo = (int)(S.lohi[0] & 0xffffu);
+        int chi = g.hi(i0 + nact - 1);
+        int lo7 = (int)(S.lohi[STRIP - 1] & 0xffffu);
+        int hi0 = (int)(S.lohi[0] >> 16);
+        uint32_t rwA = load16(readA.arena, readA.pos + (uint64_t)(i0 - 1));
+        uint32_t rwB = load16(readB.arena, readB.pos + (uint64_t)(i0 - 1));
+        uint32_t rnA = readA.cnt ? nmask16(readA.iv, readA.cnt, i0 - 1) : 0u;
+        uint32_t rnB = readB.cnt ? nmask16(readB.iv, readB.cnt, i0 - 1) : 0u;
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            uint32_t ca = (rwA >> (30 - 2 * r)) & 3u, cb = (rwB >> (30 - 2 * r)) & 3u;
+            if ((rnA >> (31 - r)) & 1u) ca = 4;
+            if ((rnB >> (31 - r)) & 1u) cb = 4;
+            S.la[r] = s_lut[2 * ca];
+            S.lb[r] = s_lut[2 * cb];
+        }
+        uint32_t diag = 0x00020002u;
+        if (clo - 1 >= plo && clo - 1 <= phi) diag = rb[(size_t)(clo - 1 - plo) * 32].x;
+        uint32_t *ta = tbA + (size_t)s * sw * 32, *tbq = tbB + (size_t)s * sw * 32;
+        int a_end = min(lo7, chi);
+        dp_cols2<1, true>(S, oe1, oe4, ex4, clo, a_end, diag, winA, winB, rb, plo, phi, lo7, ta,
+                          tbq);
+        int b_beg = lo7 + 1, b_end = min(hi0 - 1, chi);
+        if (b_beg <= b_end)
+            dp_cols2<0, false>(S, oe1, oe4, ex4, b_beg, b_end, diag, winA, winB, rb, plo, phi,
+                               lo7, ta + (size_t)(b_beg - clo) * 32,
+                               tbq + (size_t)(b_beg - clo) * 32);
+        int c_beg = max(lo7 + 1, hi0);
+        if (c_beg <= chi)
+            dp_cols2<1, true>(S, oe1, oe4, ex4, c_beg, chi, diag, winA, winB, rb, plo, phi, lo7,
+                              ta + (size_t)(c_beg - clo) * 32, tbq + (size_t)(c_beg - clo) * 32);
+        // row bookkeeping in row order (extend.rs:795-827), per lane
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            if (r < nact) {
+                const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    FillResult &F = q ? FB : FA;
+                    int rowHp = (int)((S.rmax[r] >> (16 * q)) & 0xffffu);
+                    int argj = (int)((S.arg[r] >> (16 * q)) & 0xffffu);
+                    bool tr = (S.tright >> (8 * q + r)) & 1u;
+                    if (F.trow == 0) {
+                        if (argj == lo) {
+                            F.trow = i0 + r;
+                            F.tleft = true;
+                            F.tclamp = lo <= 1;
+                        } else if (hi < n && tr) {
+                            F.trow = i0 + r;
+                            F.tleft = false;
+                            F.tclamp = hi >= n;
+                        }
+                    }
+                    if (rowHp > F.bestHp) {
+                        F.bestHp = rowHp;
+                        F.best_i = i0 + r;
+                        F.best_j = argj;
+                    }
+                }
+            }
+        }
+        plo = lo7;
+        phi = (int)(S.lohi[STRIP - 1] >> 16);
+    }
+}
+
+// Out-of-line finish and single-pair paths for the paired kernel: their
+// registers are then not reserved across the paired fill.
+__device__ __noinline__ void finish_call(const GotohJob &job, const GotohConst &K,
+                                         const int8_t *__restrict__ lut, uint32_t pi,
+                                         PairSetup &S, const FillResult &F, const uint32_t *tb) {
+    finish_pair<32>(job, K, lut, pi, S, F, tb);
+}
+
+__device__ __noinline__ void single_call(const GotohJob &job, const GotohConst &K,
+                                         const uint32_t *__restrict__ s_lut,
+                                         const int8_t *__restrict__ lut, uint32_t pi,
+                                         PairSetup &S, uint32_t *tb, uint32_t *rb) {
+    FillResult F = S.win.cnt ? dp_fill<true>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, rb)
+                             : dp_fill<false>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, rb);
+    finish_pair<32>(job, K, lut, pi, S, F, tb);
+}
+
+// Work item (a, b): both pairs in one thread when their geometry matches and
+// their windows carry no N; otherwise one after the other (b = NONE: a alone).
+// The descriptors are resolved again after the fill rather than kept live
+// across it.
+constexpr uint32_t NO_PAIR = 0xffffffffu;
+
+__device__ void process_item2(const GotohJob &job, const GotohConst &K,
+                              const uint32_t *__restrict__ s_lut, const int8_t *__restrict__ lut,
+                              uint32_t pa, uint32_t pb, uint32_t *tb, uint32_t *rb) {
+    uint32_t *tbB = tb + job.tb_words * 32;  // second half of the thread's slot
+    bool both;
+    FillResult FA, FB;
+    {
+        PairSetup A, B;
+        const bool ra = setup_pair(job, K, pa, job.tb_words, job.rb_words, true, A);
+        const bool rb_ = pb != NO_PAIR && setup_pair(job, K, pb, job.tb_words, job.rb_words, true, B);
+        both = ra && rb_ && A.m == B.m && A.n == B.n && A.full == B.full &&
+               A.g.off == B.g.off && A.g.half == B.g.half && A.win.cnt == 0 && B.win.cnt == 0;
+        if (both) {
+            dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win, B.win, tb, tbB, A.sw,
+                     reinterpret_cast<uint2 *>(rb), FA, FB);
+        } else {
+            // One pair at a time: the row buffer is laid out for pairs (two
+            // words per lane and column), so a lone pair keeps its row buffer
+            // in the unused second traceback region (tb_words >= rb_words: a
+            // pair's traceback holds at least one strip of row-buffer width).
+            if (ra) single_call(job, K, s_lut, lut, pa, A, tb, tbB);
+            if (rb_) single_call(job, K, s_lut, lut, pb, B, tb, tbB);
+        }
+    }
+    if (both) {
+        PairSetup A, B;
+        setup_pair(job, K, pa, job.tb_words, job.rb_words, false, A);
+        finish_call(job, K, lut, pa, A, FA, tb);
+        setup_pair(job, K, pb, job.tb_words, job.rb_words, false, B);
+        finish_call(job, K, lut, pb, B, FB, tbB);
+    }
+}
+
+// Persistent paired kernel: work item k of the (class range of the) list is
+// positions 2k and 2k + 1; neighbours in the binned list share their
+// geometry key.  Scratch per warp: 2 x tb_words and 2 x rb_words words per
+// lane.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) gotoh2_kernel(GotohJob job, GotohConst K) {
+    __shared__ uint32_t s_lut[10];
+    __shared__ int8_t s_lut25[32];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) s_lut[k] = K.lut4[k >> 1][k & 1];
+#pragma unroll
+        for (int k = 0; k < 25; k++) s_lut25[k] = K.lut[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp_slot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t *tb = job.tb + warp_slot * (2 * job.tb_words) * 32 + lane;
+    uint32_t *rb = job.rb + warp_slot * (2 * job.rb_words) * 32 + 2 * lane;
+    uint64_t b0 = 0, b1 = job.list_count ? (uint64_t)(*job.list_count) : job.n_pairs;
+    if (job.range) {  // one length class of the binned list
+        b0 = job.range[0];
+        b1 = job.range[1] > job.range[0] ? job.range[1] : b0;
+    }
+    const uint64_t total = (b1 - b0 + 1) / 2;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd((unsigned long long *)job.queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        uint64_t k = base + lane;
+        if (k < total) {
+            uint64_t x = b0 + 2 * k, y = x + 1;
+            uint32_t pa = job.list ? job.list[x] : (uint32_t)x;
+            uint32_t pb = y < b1 ? (job.list ? job.list[y] : (uint32_t)y) : NO_PAIR;
+            process_item2(job, K, s_lut, s_lut25, pa, pb, tb, rb);
+        }
+    }
+}
+
 int make_gotoh_const(const esp_extend_params &p, GotohConst &k) {
     // Device domain: substitution scores fit the 4*s int8 PRMT table and the
     // scaled gap keys fit int16 in the row buffer.  The reference's own
@@ -984,15 +1311,20 @@ void gotoh_scratch_words(uint32_t m, uint32_t n, int32_t half, uint64_t &tb, uin
     rb = (uint64_t)sw;
 }
 
-// Kernel variants: resident blocks per SM requested at compile time.  More
-// blocks mean fewer registers per thread (spills) but more warps to hide
-// latency; which wins depends on the band width, so the host picks per
-// launch (see the tuning in abi.cu).
+// Kernel variants: 0, 1 = one pair per thread at 3 / 4 resident blocks per
+// SM; 2, 3 = two pairs per thread (16x2 lanes) at 3 / 4.  More blocks mean
+// fewer registers per thread (spills) but more warps to hide latency; which
+// wins depends on the band width, so the host picks per length class (the
+// tuning in abi.cu).
 int gotoh_blocks_per_sm(int block, int variant) {
     int nb = 0;
-    cudaError_t e = variant == 0
-                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel<3>, block, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel<4>, block, 0);
+    cudaError_t e;
+    switch (variant) {
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel<3>, block, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh2_kernel<3>, block, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh2_kernel<4>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gotoh_kernel<4>, block, 0);
+    }
     if (e != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
@@ -1001,8 +1333,12 @@ cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, in
                          cudaStream_t st, int variant) {
     int threads = warps * 32;
     int grid = (threads + block - 1) / block;
-    if (variant == 0) gotoh_kernel<3><<<grid, block, 0, st>>>(job, k);
-    else gotoh_kernel<4><<<grid, block, 0, st>>>(job, k);
+    switch (variant) {
+    case 0: gotoh_kernel<3><<<grid, block, 0, st>>>(job, k); break;
+    case 2: gotoh2_kernel<3><<<grid, block, 0, st>>>(job, k); break;
+    case 3: gotoh2_kernel<4><<<grid, block, 0, st>>>(job, k); break;
+    default: gotoh_kernel<4><<<grid, block, 0, st>>>(job, k);
+    }
     return cudaGetLastError();
 }
 

@@ -100,6 +100,12 @@ class ExtendBuffer:
         one warp per pair, larger ones one thread per pair; same results."""
         self.check(self._L.esp_set_warp_max(self._h, int(warp_max)))
 
+    def set_kernel_variant(self, variant: int):
+        """Thread-per-pair kernel variant: 0 / 1 one pair per thread (3 / 4
+        blocks per SM), 2 / 3 two pairs of one band geometry per thread
+        (band mode), -1 the default; same results."""
+        self.check(self._L.esp_set_kernel_variant(self._h, int(variant)))
+
     def stream_ptr(self) -> int:
         return self._L.esp_stream(self._h) or 0
 

@@ -92,6 +92,13 @@ int esp_create(esp_handle **out, int device);
  * per pair in the persistent length-binned kernel.  Both give identical
  * results.  Default 2048, or the ESP_WARP_MAX environment variable. */
 int esp_set_warp_max(esp_handle *h, long warp_max);
+/* Kernel variant of the thread-per-pair batches (no counterpart in the
+ * reference): 0 = one pair per thread at 3 resident blocks per SM, 1 = at 4
+ * blocks, 2 / 3 = two pairs of identical band geometry per thread (16x2 SIMD
+ * lanes; band-mode batches only, other batches run 0 / 1) at 3 / 4 blocks;
+ * -1 = the ESP_GOTOH_VARIANT environment variable, else 1.  Clears a
+ * previous autotuning.  All variants give identical results. */
+int esp_set_kernel_variant(esp_handle *h, int variant);
 int esp_destroy(esp_handle *h);
 /* Message of the last error on this handle (static storage of the handle). */
 const char *esp_last_error(const esp_handle *h);
@@ -184,14 +191,15 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
                           uint32_t *cigar, uint32_t cigar_stride);
 
 /* Autotuning per length class (no counterpart in the reference): runs the
- * band-mode batch once per DP kernel variant on each of four length classes
- * of its binned work list (band/window width >= 196, [100, 196), [52, 100),
- * < 52 columns), keeps the fastest variant per class for every later batch
- * of the handle (ms: 8 timings, class-major over the two variants -- 168
- * registers and 3 blocks per SM, 128 registers and 4 blocks per SM;
- * variants: the choice per class; either may be null) and leaves the batch's
- * results in out/cigar.
- * Needs a batch above the warp-per-pair size. */
+ * band-mode batch once per DP kernel variant (esp_set_kernel_variant's 0..3)
+ * on each of four length classes of its binned work list (band/window width
+ * >= 196, [100, 196), [52, 100), < 52 columns) and on the whole list in one
+ * launch.  Later band-mode batches of the handle run the fastest variant per
+ * class when the classes' best times add up to less than the best single
+ * launch, else that single launch's variant for all.  ms: 20 timings, row-
+ * major (classes 0..3, then the whole list) over the four variants;
+ * variants: the choice per class; either may be null.  The batch's results
+ * are left in out/cigar.  Needs a batch above the warp-per-pair size. */
 int esp_batch_autotune(esp_handle *h, int mode, const esp_pair *pairs, uint64_t n_pairs,
                        const uint8_t *arena, uint64_t arena_bytes, const esp_n_interval *n_iv,
                        uint64_t n_iv_count, const esp_batch_limits *limits,

@@ -23,14 +23,17 @@ _BUFS = {}
 
 
 def kernel_buffer(kind):
-    """A handle pinned to one DP kernel: 'warp' (warp per pair) or 'thread'
-    (thread per pair, length binned); None = the size-based default."""
+    """A handle pinned to one DP kernel: 'warp' (warp per pair), 'thread'
+    (thread per pair, length binned) or 'paired' (two pairs of one band
+    geometry per thread, band mode); None = the size-based default."""
     if kind is None:
         return None
     if kind not in _BUFS:
         from esperanto_gb300.extend import ExtendBuffer
         b = ExtendBuffer()
         b.set_warp_max(1 << 40 if kind == "warp" else 0)
+        if kind == "paired":
+            b.set_kernel_variant(2)
         _BUFS[kind] = b
     return _BUFS[kind]
 
@@ -58,11 +61,15 @@ def gpu_batch(cases, edit_dir, mode=B.MODE_BAND, cigar_stride=None, kernel=None)
     return res
 
 
-def compare(cases, edit_dirs, mode=B.MODE_BAND, ctxs=None, kernels=("thread", "warp")):
+def compare(cases, edit_dirs, mode=B.MODE_BAND, ctxs=None,
+            kernels=("thread", "warp", "paired")):
     """Run cases grouped by edit_dir through GPU (each DP kernel) and the
-    oracle; assert equality."""
+    oracle; assert equality.  The paired kernel runs band-mode batches only
+    (hint batches on that handle run the one-pair kernel)."""
     n = 0
     for kern in kernels:
+        if kern == "paired" and mode != B.MODE_BAND:
+            continue
         n = _compare(cases, edit_dirs, mode, ctxs, kern)
     return n
 

@@ -15,7 +15,7 @@ if not torch.cuda.is_available():
 
 import esperanto_gb300 as E  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
-from gpu_helpers import compare  # noqa: E402
+from gpu_helpers import compare, kernel_buffer  # noqa: E402
 
 
 def _gpu_kind(kind, case):
@@ -216,8 +216,73 @@ def test_graph_replay_of_identical_device_batches():
             assert (cig[k, :out[k]["n_ops"]] == wc[k, :out[k]["n_ops"]]).all()
 
 
+def _geometry_groups(seed, groups, per_group):
+    """Cases in groups of one band geometry (read length, window length,
+    offset, half): what the paired kernel runs two to a thread.  Reads are
+    mutated window slices; some reads and some windows carry N."""
+    rng = np.random.default_rng(seed)
+    cases, ctx = [], []
+    for gi, (m, n, off, half) in enumerate(groups):
+        for k in range(per_group):
+            win = rng.choice(list("ACGT"), n)
+            s = int(rng.integers(0, max(1, n - m + 1)))
+            read = list(win[s:s + m]) + list(rng.choice(list("ACGT"), max(0, m - (n - s))))
+            read = read[:m]
+            for _ in range(int(rng.integers(0, 6))):  # substitutions, indels
+                if not read:
+                    break
+                q = int(rng.integers(0, len(read)))
+                kind = int(rng.integers(0, 3))
+                if kind == 0:
+                    read[q] = str(rng.choice(list("ACGT")))
+                elif kind == 1:
+                    read.insert(q, str(rng.choice(list("ACGT"))))
+                    read.pop()
+                else:
+                    read.pop(q)
+                    read.append(str(rng.choice(list("ACGT"))))
+            if k % 7 == 3 and m > 2:
+                read[m // 2] = "N"
+            if k % 5 == 1:  # a window N: this pair runs alone
+                win[n // 3] = "N"
+            cases.append(("".join(read).encode(), "".join(win).encode(),
+                          (off, half) if half >= 0 else None))
+            ctx.append(f"group {gi} {(m, n, off, half)} pair {k}")
+    return cases, ctx
+
+
+def test_paired_kernel_geometry_groups():
+    """Two pairs per thread (16x2 lanes): groups of identical geometry --
+    single strips, ragged last strips, clamped band edges, full matrices --
+    with odd group sizes so some neighbours differ and run one after the
+    other; every pair matches the oracle."""
+    groups = [(1, 5, 0, 2), (7, 20, 3, 4), (8, 40, 2, 16), (9, 60, 16, 16), (31, 95, 32, 32),
+              (150, 214, 32, 32), (150, 150, -20, 16), (64, 300, 250, 8), (301, 301, 0, 64),
+              (40, 50, 0, -1), (17, 33, 0, -1), (100, 230, 65, 64), (250, 510, 128, 128)]
+    cases, ctx = _geometry_groups(5, groups, 37)
+    dirs = [k % 3 for k in range(len(cases))]
+    assert compare(cases, dirs, ctxs=ctx, kernels=("paired",)) == len(cases)
+
+
+def test_paired_kernel_variants_on_mixed_batch():
+    """Both paired variants (3 and 4 blocks per SM) on the mixed-length
+    workload equal the one-pair kernel bit for bit (results and CIGARs)."""
+    from esperanto_gb300.extend import ExtendBuffer
+    ar, pr = B.synth_gotoh(31, 50000, 2)
+    want = B.extend_batch_host(pr, ar, cigar_stride=32, buf=kernel_buffer("thread"))
+    for v in (2, 3):
+        buf = ExtendBuffer()
+        buf.set_warp_max(0)
+        buf.set_kernel_variant(v)
+        out, cig = B.extend_batch_host(pr, ar, cigar_stride=32, buf=buf)
+        assert (out == want[0]).all(), v
+        for k in range(len(pr)):
+            nops = int(out[k]["n_ops"])
+            assert (cig[k, :nops] == want[1][k, :nops]).all(), (v, k)
+
+
 def test_autotune_per_length_class():
-    """Autotuning times both DP variants per length class, keeps the fastest,
+    """Autotuning times every DP variant per length class, keeps the fastest,
     and later batches (per-class launches, then a captured graph) give the
     same results as the untuned path."""
     import ctypes as C
@@ -234,11 +299,11 @@ def test_autotune_per_length_class():
     d_out = torch.zeros(n * B.EXT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     d_cig = torch.zeros(n * 32, dtype=torch.int32, device="cuda")
     variants = (C.c_int * 4)()
-    ms = (C.c_double * 8)()
+    ms = (C.c_double * 20)()
     args = (buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n, d_arena.data_ptr(), ar.nbytes, None,
             0, C.byref(lim), C.byref(p), d_out.data_ptr(), d_cig.data_ptr(), 32, None)
     buf.check(N.lib().esp_batch_autotune(*args, variants, ms))
-    assert all(v in (0, 1) for v in variants) and all(x > 0 for x in ms)
+    assert all(v in (0, 1, 2, 3) for v in variants) and all(x > 0 for x in ms)
     for it in range(4):  # per-class launches, then capture and replays
         if it:
             d_out.zero_()
