@@ -71,7 +71,7 @@ struct Seq {
 };
 
 struct Strip {
-    int Hl[STRIP], Fl[STRIP], rk[STRIP], hr[STRIP];
+    int Hl[STRIP], Fl[STRIP], rk[STRIP];
     uint32_t l0[STRIP], l1[STRIP];
     int lo[STRIP], hi[STRIP];
 };
@@ -106,23 +106,28 @@ __device__ __forceinline__ uint32_t dp_column(Strip &S, const GotohConst &K, int
         wb = mad_u32(wb, 4u, (uint32_t)((kE & 1) | (kF & 2)));
         int rkey = (int)mad_u32((uint32_t)Hp, 32768u, cj);
         if (MASK) {
-            bool in = (j >= S.lo[r]) & (j <= S.hi[r]);
-            if (j == S.hi[r]) S.hr[r] = Hp;
+            // An out-of-window cell shows H = 0, E = NEG to the row below and
+            // leaves its row's state alone: before the window that is still
+            // the start state, after it Hl keeps H at the window's last
+            // column (the strip's bookkeeping reads it; the cells of the row
+            // below that follow are out of their window too, as hi(i+1) <=
+            // hi(i) + 1).
+            const bool in = (j >= S.lo[r]) & (j <= S.hi[r]);
             if (in) {
                 S.rk[r] = max(S.rk[r], rkey);
-            } else {
-                Hp = 2;
-                E4 = NEG4;
-                F4 = NEG4;
+                S.Hl[r] = Hp;
+                S.Fl[r] = F4;
             }
+            upH = in ? Hp : 2;
+            upE = in ? E4 : NEG4;
         } else {
             S.rk[r] = max(S.rk[r], rkey);
+            S.Hl[r] = Hp;
+            S.Fl[r] = F4;
+            upH = Hp;
+            upE = E4;
         }
         d = left;
-        S.Hl[r] = Hp;
-        S.Fl[r] = F4;
-        upH = Hp;
-        upE = E4;
     }
     return __byte_perm(wa, wb, 0x5410);
 }
@@ -226,7 +231,6 @@ __device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ 
             S.Hl[r] = 2;
             S.Fl[r] = NEG4;
             S.rk[r] = -1;
-            S.hr[r] = -1;
         }
         int clo = S.lo[0];
         int chi = g.hi(i0 + nact - 1);
@@ -267,7 +271,7 @@ __device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ 
                         R.trow = i0 + r;
                         R.tleft = true;
                         R.tclamp = S.lo[r] <= 1;
-                    } else if (S.hi[r] < n && S.hr[r] == rowHp) {
+                    } else if (S.hi[r] < n && S.Hl[r] == rowHp) {
                         R.trow = i0 + r;
                         R.tleft = false;
                         R.tclamp = S.hi[r] >= n;
@@ -800,7 +804,6 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
             S.Hl[r] = 2;
             S.Fl[r] = NEG4;
             S.rk[r] = -1;
-            S.hr[r] = -1;
         }
         const int clo = S.lo[0];
         const int chi = act ? g.hi(i0 + nact - 1) : 0;
@@ -869,7 +872,7 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
                         trow = i0 + r;
                         tleft = true;
                         tclamp = S.lo[r] <= 1;
-                    } else if (S.hi[r] < n && S.hr[r] == rowHp) {
+                    } else if (S.hi[r] < n && S.Hl[r] == rowHp) {
                         trow = i0 + r;
                         tleft = false;
                         tclamp = S.hi[r] >= n;
@@ -959,7 +962,6 @@ struct Strip2 {
     uint32_t la[STRIP], lb[STRIP];
     uint32_t arg[STRIP];   // first column of the row maximum: pair A low half, B high
     uint32_t lohi[STRIP];  // row window: first column low half, last column high half
-    uint32_t tright;       // bit r (A) / 8 + r (B): H at the row's last column is the max
 };
 
 __device__ __forceinline__ uint32_t prmt(uint32_t lo, uint32_t hi, uint32_t sel) {
@@ -1000,28 +1002,24 @@ __device__ __forceinline__ void dp_column2(Strip2 &S, const uint32_t oe1, const 
         uint32_t Hp = (key & KEEP2) | 0x00020002u;
         wa = mad_u32(wa, 4u, key & 0x00030003u);
         wb = mad_u32(wb, 4u, (kE & 0x00010001u) | (kF & 0x00020002u));
-        if (MASK) {
+        if (MASK) {  // out-of-window cells: as in dp_column
             const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
-            if ((j >= lo) & (j <= hi)) {
+            const bool in = (j >= lo) & (j <= hi);
+            if (in) {
                 row_max2(S.rmax[r], S.arg[r], Hp, jj);
-                if (j == hi) {  // the row's last column: is its H the row maximum?
-                    uint32_t eq = S.rmax[r] ^ Hp;
-                    if ((eq & 0xffffu) == 0) S.tright |= 1u << r;
-                    if ((eq >> 16) == 0) S.tright |= 0x100u << r;
-                }
-            } else {
-                Hp = 0x00020002u;
-                E4 = NEG2;
-                F4 = NEG2;
+                S.Hl[r] = Hp;
+                S.Fl[r] = F4;
             }
+            upH = in ? Hp : 0x00020002u;
+            upE = in ? E4 : NEG2;
         } else {
             row_max2(S.rmax[r], S.arg[r], Hp, jj);
+            S.Hl[r] = Hp;
+            S.Fl[r] = F4;
+            upH = Hp;
+            upE = E4;
         }
         d = left;
-        S.Hl[r] = Hp;
-        S.Fl[r] = F4;
-        upH = Hp;
-        upE = E4;
     }
 }
 
@@ -1101,7 +1099,6 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
             S.rmax[r] = 0u;
             S.arg[r] = 0u;
         }
-        S.tright = 0u;
         int clo = (int)(S.lohi[0] & 0xffffu);
         int chi = g.hi(i0 + nact - 1);
         int lo7 = (int)(S.lohi[STRIP - 1] & 0xffffu);
@@ -1143,7 +1140,7 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
                     FillResult &F = q ? FB : FA;
                     int rowHp = (int)((S.rmax[r] >> (16 * q)) & 0xffffu);
                     int argj = (int)((S.arg[r] >> (16 * q)) & 0xffffu);
-                    bool tr = (S.tright >> (8 * q + r)) & 1u;
+                    bool tr = (((S.rmax[r] ^ S.Hl[r]) >> (16 * q)) & 0xffffu) == 0;
                     if (F.trow == 0) {
                         if (argj == lo) {
                             F.trow = i0 + r;
@@ -1168,20 +1165,37 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
     }
 }
 
-// Out-of-line finish and single-pair paths for the paired kernel: their
-// registers are then not reserved across the paired fill.
+// Out-of-line fill, finish and lone-pair paths of the paired kernel: one
+// copy of each in the kernel's code, and their registers are not reserved
+// across one another.
+__device__ __noinline__ void fill2_call(const GotohConst &K, const uint32_t *__restrict__ s_lut,
+                                        const PairSetup &A, const PairSetup &B, uint32_t *tbA,
+                                        uint32_t *tbB, uint32_t *rb, FillResult &FA,
+                                        FillResult &FB) {
+    dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win, B.win, tbA, tbB, A.sw,
+             reinterpret_cast<uint2 *>(rb), FA, FB);
+}
+
 __device__ __noinline__ void finish_call(const GotohJob &job, const GotohConst &K,
                                          const int8_t *__restrict__ lut, uint32_t pi,
                                          PairSetup &S, const FillResult &F, const uint32_t *tb) {
     finish_pair<32>(job, K, lut, pi, S, F, tb);
 }
 
-__device__ __noinline__ void single_call(const GotohJob &job, const GotohConst &K,
-                                         const uint32_t *__restrict__ s_lut,
-                                         const int8_t *__restrict__ lut, uint32_t pi,
-                                         PairSetup &S, uint32_t *tb, uint32_t *rb) {
-    FillResult F = S.win.cnt ? dp_fill<true>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, rb)
-                             : dp_fill<false>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, rb);
+// A pair without a partner of its geometry: the paired fill with itself in
+// both lanes (the second lane's traceback lands in the slot's unused half),
+// or, when its window has N (the paired fill takes N in reads only), the
+// one-pair fill with its row buffer in that unused half (tb_words >=
+// rb_words: a pair's traceback holds at least one strip of row-buffer width).
+__device__ __noinline__ void lone_call(const GotohJob &job, const GotohConst &K,
+                                       const uint32_t *__restrict__ s_lut,
+                                       const int8_t *__restrict__ lut, uint32_t pi,
+                                       PairSetup &S, uint32_t *tb, uint32_t *tbB, uint32_t *rb) {
+    FillResult F, F2;
+    if (S.win.cnt)
+        F = dp_fill<true>(K, s_lut, S.m, S.n, S.g, S.read, S.win, tb, S.sw, tbB);
+    else
+        fill2_call(K, s_lut, S, S, tb, tbB, rb, F, F2);
     finish_pair<32>(job, K, lut, pi, S, F, tb);
 }
 
@@ -1204,15 +1218,10 @@ __device__ void process_item2(const GotohJob &job, const GotohConst &K,
         both = ra && rb_ && A.m == B.m && A.n == B.n && A.full == B.full &&
                A.g.off == B.g.off && A.g.half == B.g.half && A.win.cnt == 0 && B.win.cnt == 0;
         if (both) {
-            dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win, B.win, tb, tbB, A.sw,
-                     reinterpret_cast<uint2 *>(rb), FA, FB);
+            fill2_call(K, s_lut, A, B, tb, tbB, rb, FA, FB);
         } else {
-            // One pair at a time: the row buffer is laid out for pairs (two
-            // words per lane and column), so a lone pair keeps its row buffer
-            // in the unused second traceback region (tb_words >= rb_words: a
-            // pair's traceback holds at least one strip of row-buffer width).
-            if (ra) single_call(job, K, s_lut, lut, pa, A, tb, tbB);
-            if (rb_) single_call(job, K, s_lut, lut, pb, B, tb, tbB);
+            if (ra) lone_call(job, K, s_lut, lut, pa, A, tb, tbB, rb);
+            if (rb_) lone_call(job, K, s_lut, lut, pb, B, tb, tbB, rb);
         }
     }
     if (both) {
