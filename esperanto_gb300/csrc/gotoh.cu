@@ -82,6 +82,20 @@ __device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) 
     return d;
 }
 
+// a & m and (a & m) | o as opaque logic ops, so that the compiler keeps the
+// differences below as adds instead of folding them back into logic.
+__device__ __forceinline__ uint32_t and_u32(uint32_t a, uint32_t m) {
+    uint32_t d;
+    asm("and.b32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(m));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t and_or_u32(uint32_t a, uint32_t m, uint32_t o) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0xEA;" : "=r"(d) : "r"(a), "r"(m), "r"(o));
+    return d;
+}
+
 // One column of one strip.  upH/upE enter as the row above the strip at
 // column j and leave as the strip's last row at column j; `diag` is the row
 // above at column j-1; cj = 32767 - j (row-max key tie order).  MASK = 1
@@ -97,13 +111,17 @@ __device__ __forceinline__ uint32_t dp_column(Strip &S, const GotohConst &K, int
         int left = S.Hl[r];
         int kE = max(upE + K.ex4, upH + K.oe1);
         int kF = max(S.Fl[r] + K.ex4, left + K.oe4);
-        int E4 = kE & ~3;
-        int F4 = kF & ~3;
+        // kE = 0 or 1 and kF = 0 or 2 (mod 4): the opened flags are kE - E4
+        // and kF - F4, the E tag is E4 + 1, the key's tag key - Hp + 2 --
+        // adds, which also issue on the FMA pipe, instead of logic ops on
+        // the saturated ALU pipe
+        int E4 = (int)and_u32((uint32_t)kE, ~3u);
+        int F4 = (int)and_u32((uint32_t)kF, ~3u);
         int kd = max(d + prmt_sx(S.l0[r], S.l1[r], sel), 3);  // START tag 3 folded in
-        int key = max(max(kd, kE | 1), F4);
-        int Hp = (key & ~3) | 2;
-        wa = mad_u32(wa, 4u, (uint32_t)(key & 3));
-        wb = mad_u32(wb, 4u, (uint32_t)((kE & 1) | (kF & 2)));
+        int key = max(max(kd, E4 + 1), F4);
+        int Hp = (int)and_or_u32((uint32_t)key, ~3u, 2u);
+        wa = mad_u32(wa, 4u, (uint32_t)(key - Hp + 2));
+        wb = mad_u32(wb, 4u, (uint32_t)((kE - E4) + (kF - F4)));
         int rkey = (int)mad_u32((uint32_t)Hp, 32768u, cj);
         if (MASK) {
             // An out-of-window cell shows H = 0, E = NEG to the row below and
@@ -995,13 +1013,16 @@ __device__ __forceinline__ void dp_column2(Strip2 &S, const uint32_t oe1, const 
         uint32_t left = S.Hl[r];
         uint32_t kE = __viaddmax_s16x2(upE, ex4, __viaddmax_s16x2(upH, oe1, VNEG2));
         uint32_t kF = __viaddmax_s16x2(S.Fl[r], ex4, __viaddmax_s16x2(left, oe4, VNEG2));
-        uint32_t E4 = kE & KEEP2;
-        uint32_t F4 = kF & KEEP2;
+        // tags and flags by adds as in dp_column: every half's result is in
+        // [0, 3] (E4 + 1 cannot carry: E4's low bits are 0), so the packed
+        // 32-bit adds are exact per half
+        uint32_t E4 = and_u32(kE, KEEP2);
+        uint32_t F4 = and_u32(kF, KEEP2);
         uint32_t kd = __viaddmax_s16x2(d, prmt(S.la[r], S.lb[r], sel), 0x00030003u);
-        uint32_t key = __vimax3_s16x2(kd, kE | 0x00010001u, F4);
-        uint32_t Hp = (key & KEEP2) | 0x00020002u;
-        wa = mad_u32(wa, 4u, key & 0x00030003u);
-        wb = mad_u32(wb, 4u, (kE & 0x00010001u) | (kF & 0x00020002u));
+        uint32_t key = __vimax3_s16x2(kd, E4 + 0x00010001u, F4);
+        uint32_t Hp = and_or_u32(key, KEEP2, 0x00020002u);
+        wa = mad_u32(wa, 4u, key - Hp + 0x00020002u);
+        wb = mad_u32(wb, 4u, (kE - E4) + (kF - F4));
         if (MASK) {  // out-of-window cells: as in dp_column
             const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
             const bool in = (j >= lo) & (j <= hi);
