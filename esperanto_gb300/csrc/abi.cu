@@ -140,19 +140,24 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         return rc;
     CK(h, cudaMemsetAsync(h->d_ctr, 0, 256, st));
     const uint32_t *order = nullptr;
+    const uint32_t *list_len = nullptr;  // device word: length of a padded list
     if (h->binning && n_pairs > 32) {
+        // the paired kernels want each geometry bin at an even list offset
+        const uint64_t slots = n_pairs + (paired ? esp::bin_pad_slots(n_pairs) : 0);
         if ((rc = grow_device(h, (void **)&h->d_hist, &h->d_hist_cap, esp::bin_scratch_bytes())) != ESP_OK)
             return rc;
-        if ((rc = grow_device(h, (void **)&h->d_order, &h->d_order_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
+        if ((rc = grow_device(h, (void **)&h->d_order, &h->d_order_cap, slots * sizeof(uint32_t))) != ESP_OK)
             return rc;
         CK(h, esp::launch_binning(d_pairs, n_pairs, mode == ESP_MODE_HINT ? 1 : 0, h->d_hist,
-                                  h->d_order, h->num_sms, st,
-                                  per_class ? h->d_ctr + 24 : nullptr));
-        h->launches += per_class ? 6 : 5;
+                                  h->d_order, h->num_sms, st, h->d_ctr + 29,
+                                  per_class ? h->d_ctr + 24 : nullptr, paired));
+        h->launches += 6 + (per_class ? 1 : 0) + (paired ? 1 : 0);
         order = h->d_order;
+        if (paired) list_len = h->d_ctr + 29;
     }
     esp::GotohJob job{};
     job.list = order;
+    job.list_count = list_len;
     job.pairs = d_pairs;
     job.n_pairs = n_pairs;
     job.arena = d_arena;

@@ -85,16 +85,33 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_w
     return wpre + x - v;
 }
 
+// PAD: every bin's slot count rounded up to even, so that list positions
+// 2k, 2k + 1 never straddle two bins; the spare slot of an odd bin holds
+// NO_PAIR (the list is pre-filled with it).
+__device__ __forceinline__ uint4 bin_counts(uint4 q, bool pad) {
+    if (pad) {
+        q.x += q.x & 1u;
+        q.y += q.y & 1u;
+        q.z += q.z & 1u;
+        q.w += q.w & 1u;
+    }
+    return q;
+}
+
+template <bool PAD>
 __global__ void __launch_bounds__(256) bin_scan_up(const uint32_t *__restrict__ hist,
                                                    uint32_t *__restrict__ part) {
     __shared__ uint32_t s_warp[8];
-    uint4 q = reinterpret_cast<const uint4 *>(hist + (size_t)blockIdx.x * SCAN_TILE)[threadIdx.x];
+    uint4 q = bin_counts(
+        reinterpret_cast<const uint4 *>(hist + (size_t)blockIdx.x * SCAN_TILE)[threadIdx.x], PAD);
     uint32_t total;
     block_excl_scan256(q.x + q.y + q.z + q.w, s_warp, total);
     if (threadIdx.x == 0) part[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(1024) bin_scan_top(uint32_t *__restrict__ part) {
+// Also writes the list length (the sum of all slots) to *total.
+__global__ void __launch_bounds__(1024) bin_scan_top(uint32_t *__restrict__ part,
+                                                     uint32_t *__restrict__ total) {
     __shared__ uint32_t s[1024];
     uint32_t v = threadIdx.x < SCAN_BLOCKS ? part[threadIdx.x] : 0;
     s[threadIdx.x] = v;
@@ -106,13 +123,15 @@ __global__ void __launch_bounds__(1024) bin_scan_top(uint32_t *__restrict__ part
         __syncthreads();
     }
     if (threadIdx.x < SCAN_BLOCKS) part[threadIdx.x] = s[threadIdx.x] - v;
+    if (threadIdx.x == 1023) *total = s[1023];
 }
 
+template <bool PAD>
 __global__ void __launch_bounds__(256) bin_scan_down(uint32_t *__restrict__ hist,
                                                      const uint32_t *__restrict__ part) {
     __shared__ uint32_t s_warp[8];
     uint4 *tile = reinterpret_cast<uint4 *>(hist + (size_t)blockIdx.x * SCAN_TILE);
-    uint4 q = tile[threadIdx.x];
+    uint4 q = bin_counts(tile[threadIdx.x], PAD);
     uint32_t total;
     uint32_t run = part[blockIdx.x] + block_excl_scan256(q.x + q.y + q.z + q.w, s_warp, total);
     uint4 r;
@@ -181,10 +200,12 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
 
 size_t bin_scratch_bytes() { return (size_t)(NBINS + SCAN_BLOCKS) * sizeof(uint32_t); }
 
+uint64_t bin_pad_slots(uint64_t n) { return n < (uint64_t)NBINS ? n : (uint64_t)NBINS; }
+
 // Length classes of the binned list (descending cost): band/window width
 // w >= 196, [100, 196), [52, 100), < 52 columns.  bounds[s], bounds[s+1] is
 // class s; read from the scanned histogram before the scatter moves it.
-__global__ void class_bounds(const uint32_t *__restrict__ hist, uint64_t n,
+__global__ void class_bounds(const uint32_t *__restrict__ hist, const uint32_t *__restrict__ total,
                              uint32_t *__restrict__ bounds) {
     if (threadIdx.x == 0) {
         const uint32_t top = (1u << KEY_BITS) - 1;
@@ -192,22 +213,27 @@ __global__ void class_bounds(const uint32_t *__restrict__ hist, uint64_t n,
         bounds[0] = 0;
         for (int s = 0; s < 3; s++)
             bounds[s + 1] = hist[NBINS - 1 - ((first_w[s] << KEY_BITS) | top)];
-        bounds[4] = (uint32_t)n;
+        bounds[4] = *total;
     }
 }
 
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
-                           uint32_t *order, int num_sms, cudaStream_t st, uint32_t *bounds) {
+                           uint32_t *order, int num_sms, cudaStream_t st, uint32_t *total,
+                           uint32_t *bounds, bool pad) {
     cudaError_t e = cudaMemsetAsync(hist, 0, bin_scratch_bytes(), st);
+    if (e == cudaSuccess && pad)
+        e = cudaMemsetAsync(order, 0xff, (n + bin_pad_slots(n)) * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     int grid = num_sms * 4;
     uint64_t need = (n + 255) / 256;
     if ((uint64_t)grid > need) grid = (int)(need ? need : 1);
     bin_hist<<<grid, 256, 0, st>>>(pairs, n, mode, hist);
-    bin_scan_up<<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
-    bin_scan_top<<<1, 1024, 0, st>>>(hist + NBINS);
-    bin_scan_down<<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
-    if (bounds) class_bounds<<<1, 32, 0, st>>>(hist, n, bounds);
+    if (pad) bin_scan_up<true><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
+    else bin_scan_up<false><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
+    bin_scan_top<<<1, 1024, 0, st>>>(hist + NBINS, total);
+    if (pad) bin_scan_down<true><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
+    else bin_scan_down<false><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
+    if (bounds) class_bounds<<<1, 32, 0, st>>>(hist, total, bounds);
     bin_scatter<<<grid, 256, 0, st>>>(pairs, n, mode, hist, order);
     return cudaGetLastError();
 }

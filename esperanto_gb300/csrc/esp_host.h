@@ -44,7 +44,8 @@ struct esp_handle {
     uint32_t *d_esc = nullptr;  // escalation list
     size_t d_esc_cap = 0;       // bytes
     // d_ctr (256 B): u64 queues at [0..1] (attempt 1), [2..3] (attempt 2),
-    // u32 esc count at [4], u64 class queues at [8..15], class bounds at [24..28]
+    // u32 esc count at [4], u64 class queues at [8..15], class bounds at
+    // [24..28], binned list length at [29]
     uint32_t *d_ctr = nullptr;
     int tune[esp::kLengthClasses] = {-1, -1, -1, -1};  // DP variant per length class (autotuned)
     bool tuned = false;

@@ -137,12 +137,17 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
                                int mode, unsigned long long *cells, int num_sms,
                                cudaStream_t st);
 
-// Counting-sort the pairs by geometry (descending cost) into `order`.
-// `hist` needs bin_scratch_bytes() of device memory.  4 launches.
+// Counting-sort the pairs by geometry (descending cost) into `order`; the
+// list length goes to *total (device).  `hist` needs bin_scratch_bytes() of
+// device memory.  6 launches (+1 with bounds, +1 memset with pad).
 // bounds (optional, 5 device words): the four length classes of the list.
+// pad: every bin padded to an even slot count with NO_PAIR entries (order
+// needs n + bin_pad_slots(n) words), for the two-pairs-per-thread kernel.
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
-                           uint32_t *order, int num_sms, cudaStream_t st,
-                           uint32_t *bounds = nullptr);
+                           uint32_t *order, int num_sms, cudaStream_t st, uint32_t *total,
+                           uint32_t *bounds = nullptr, bool pad = false);
+// Spare slots a padded list may add to n pairs (the list holds n + this).
+uint64_t bin_pad_slots(uint64_t n);
 constexpr int kLengthClasses = 4;
 size_t bin_scratch_bytes();
 

@@ -1148,6 +1148,10 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
                                lo7, ta + (size_t)(b_beg - clo) * 32,
                                tbq + (size_t)(b_beg - clo) * 32);
         int c_beg = max(lo7 + 1, hi0);
+        // the row windows again rather than kept live across the interior
+#pragma unroll
+        for (int r = 0; r < STRIP; r++)
+            S.lohi[r] = (uint32_t)g.lo(i0 + r) | ((uint32_t)g.hi(i0 + r) << 16);
         if (c_beg <= chi)
             dp_cols2<1, true>(S, oe1, oe4, ex4, c_beg, chi, diag, winA, winB, rb, plo, phi, lo7,
                               ta + (size_t)(c_beg - clo) * 32, tbq + (size_t)(c_beg - clo) * 32);
