@@ -469,14 +469,15 @@ static void merge(ScanOut &into, const ScanOut &s) {
     into.arena_end = std::max(into.arena_end, s.arena_end);
 }
 
-// Per-chunk scans (chunk c = pairs [bounds[c], bounds[c+1])), in parallel.
-static void scan_chunks(int mode, const esp_pair *pairs, const std::vector<uint64_t> &bounds,
-                        std::vector<ScanOut> &out) {
+// Per-chunk scans (chunk c = pairs [bounds[c], bounds[c+1])), in parallel
+// on the handle's host pool for batches of 32K pairs and more.
+static void scan_chunks(esp_handle *h, int mode, const esp_pair *pairs,
+                        const std::vector<uint64_t> &bounds, std::vector<ScanOut> &out) {
     const size_t C = bounds.size() - 1;
     out.assign(C, ScanOut{});
     const uint64_t n = bounds.back();
-    unsigned T = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    if (n < (1u << 16)) T = 1;
+    unsigned T = n < (1u << 15) ? 1 : (unsigned)std::min<uint64_t>(16, n >> 14);
+    if (T > 1) T = std::min(T, host_pool(h).size());
     // split every chunk into T slices; each worker scans slice t of every chunk
     std::vector<std::vector<ScanOut>> part(T, std::vector<ScanOut>(C));
     auto work = [&](unsigned t) {
@@ -485,10 +486,8 @@ static void scan_chunks(int mode, const esp_pair *pairs, const std::vector<uint6
             scan_range(mode, pairs, a + len * t / T, a + len * (t + 1) / T, part[t][c]);
         }
     };
-    std::vector<std::thread> th;
-    for (unsigned t = 1; t < T; t++) th.emplace_back(work, t);
-    work(0);
-    for (auto &x : th) x.join();
+    if (T > 1) host_pool(h).run(T, work);
+    else work(0);
     for (unsigned t = 0; t < T; t++)
         for (size_t c = 0; c < C; c++) merge(out[c], part[t][c]);
 }
@@ -514,7 +513,7 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     std::vector<uint64_t> bounds(C + 1);
     for (uint64_t c = 0; c <= C; c++) bounds[c] = n_pairs * c / C;
     std::vector<ScanOut> sc;
-    scan_chunks(mode, pairs, bounds, sc);
+    scan_chunks(h, mode, pairs, bounds, sc);
     ScanOut all;
     for (auto &s : sc) merge(all, s);
     const Limits &L1 = all.L1, &L2 = all.L2;

@@ -178,8 +178,8 @@ int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
     // scanned by several host threads
     uint32_t mx = 1;
     {
-        unsigned T = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        if (n_pairs < (1u << 16)) T = 1;
+        unsigned T = n_pairs < (1u << 16) ? 1 : (unsigned)std::min<uint64_t>(16, n_pairs >> 15);
+        if (T > 1) T = std::min(T, host_pool(h).size());
         std::vector<uint32_t> part(T, 1);
         auto work = [&](unsigned t) {
             uint32_t m = 1;
@@ -187,10 +187,8 @@ int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
                 m = std::max(m, pairs[k].read_len);
             part[t] = m;
         };
-        std::vector<std::thread> th;
-        for (unsigned t = 1; t < T; t++) th.emplace_back(work, t);
-        work(0);
-        for (auto &x : th) x.join();
+        if (T > 1) host_pool(h).run(T, work);
+        else work(0);
         for (uint32_t m : part) mx = std::max(mx, m);
     }
     if (mx > (uint32_t)LONG_MAX_M) return fail(h, ESP_EINVAL, "Myers read length must be <= 256");

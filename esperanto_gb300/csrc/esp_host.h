@@ -7,13 +7,17 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "esp_internal.h"
 #include "esperanto_gb300.h"
+#include "host_pool.h"
 
 struct esp_handle {
+    std::unique_ptr<HostPool> pool;  // host scan threads, started on first use
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
@@ -157,6 +161,15 @@ struct Limits {
     uint64_t tb_words = 1, rb_words = 1;
     uint32_t max_m = 0;
 };
+
+// The handle's host worker pool (up to 16 threads with the caller).
+inline HostPool &host_pool(esp_handle *h) {
+    if (!h->pool) {
+        unsigned T = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        h->pool.reset(new HostPool(T - 1));
+    }
+    return *h->pool;
+}
 
 inline void add_limits(Limits &L, uint32_t m, uint32_t n, int32_t half) {
     uint64_t tb, rb;
