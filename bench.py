@@ -34,11 +34,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Integer-ALU-pipe ops per cell of the DP recurrence as written in
-# csrc/gotoh.cu (E 3, F 3, tag clears 2, LUT select + diag add + floor 3,
-# H key 3, H tag 1, traceback-bit selects 2, row max 1); the three
-# multiply-adds per cell (traceback accumulators, row-max key) issue on the
-# FMA pipe and are not counted.
+# Integer ops per cell of the DP recurrence in its scalar 32-bit form (E 3,
+# F 3, tag clears 2, LUT select + diag add + floor 3, H key 3, H tag 1,
+# traceback-bit selects 2, row max 1; the multiply-adds that accumulate the
+# traceback words are not counted): the algorithmic work of one cell.  The
+# two-pairs-per-thread kernel does it in 16-bit SIMD halves, two cells per
+# 32-bit lane-op, so its roofline peak is twice the 32-bit lane-op rate.
 OPS_PER_CELL = 18
 # Myers: 10 32-bit logic/add/shift ops per 32-cell limb per text column.
 MYERS_OPS_PER_CELL = 10.0 / 32.0
@@ -56,14 +57,24 @@ DEFAULT_PAIRS = {0: 65536, 1: 1048576, 2: 4194304, 3: 524288}
 SEEDS = {0: 1, 1: 2, 2: 3, 3: 4}
 
 
-def int_peak(L, buf):
+def int_peak(L, buf, lanes=1):
     """Measured integer-ALU issue peak of this GPU (lane-ops/s): the slower
-    of the 3-input-logic and integer-max probe streams (esp_int_peaks)."""
+    of the 3-input-logic and integer-max probe streams (esp_int_peaks); for
+    the 16x2 SIMD kernel (lanes = 2) the slowest of those and the 16x2
+    add-max / 3-way-max streams (esp_simd16_peaks), times two 16-bit cells
+    per lane-op."""
     v = [C.c_double() for _ in range(4)]
     buf.check(L.esp_int_peaks(buf.handle, *[C.byref(x) for x in v]))
     lop3, imnmx, iadd, imad = (x.value for x in v)
-    return min(lop3, imnmx), {"lop3": lop3 / 1e12, "imnmx": imnmx / 1e12,
-                              "iadd": iadd / 1e12, "imad": imad / 1e12}
+    probe = {"lop3": lop3 / 1e12, "imnmx": imnmx / 1e12, "iadd": iadd / 1e12,
+             "imad": imad / 1e12}
+    peak = min(lop3, imnmx)
+    if lanes == 2:
+        s = [C.c_double() for _ in range(2)]
+        buf.check(L.esp_simd16_peaks(buf.handle, *[C.byref(x) for x in s]))
+        probe["addmax_s16x2"], probe["max3_s16x2"] = s[0].value / 1e12, s[1].value / 1e12
+        peak = 2 * min(peak, s[0].value, s[1].value)
+    return peak, probe
 
 
 def load_peaks():
@@ -185,6 +196,13 @@ class GotohWorkload(Workload):
                              "variants": list(variants),
                              "ms": [[round(ms[nv * s + v], 3) for v in range(nv)]
                                     for s in range(5)]}
+            chosen = list(variants)
+        else:
+            chosen = [int(os.environ.get("ESP_GOTOH_VARIANT", "1"))]
+        # variants 2 / 3 compute two pairs per thread in 16-bit SIMD halves
+        self.lanes = 2 if any(v >= 2 for v in chosen) else 1
+        if self.lanes == 2:
+            self.dtype = "int16x2"
 
         def step():
             buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
@@ -583,7 +601,8 @@ def main():
         return
 
     peaks, src = load_peaks()
-    peak_ops, probe = int_peak(L, buf)
+    lanes = getattr(wl, "lanes", 1)
+    peak_ops, probe = int_peak(L, buf, lanes)
     achieved_ops = wl.cells * wl.ops_per_cell / (ms / 1e3)
     traffic = None
     if config in TRAFFIC_BYTES and n_pairs == DEFAULT_PAIRS[config]:
@@ -624,7 +643,11 @@ def main():
                      "frac": achieved_ops / peak_ops, "traffic": traffic,
                      "traffic_source": TRAFFIC_SOURCE.get(config),
                      "peak_source": "measured on this GPU (esp_int_peaks: independent streams "
-                                    "of 3-input logic / integer max, the ALU-pipe issue rate)",
+                                    "of 3-input logic / integer max, the ALU-pipe issue rate)"
+                                    + ("; with the 16x2 add-max / 3-way-max streams "
+                                       "(esp_simd16_peaks) for the two-pairs-per-thread "
+                                       "kernel, x 2 cells per lane-op" if lanes == 2 else ""),
+                     "simd_lanes": lanes,
                      "probe_tops": probe, "ops_per_cell": wl.ops_per_cell,
                      "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": src},
         "plain_per_call": plain,

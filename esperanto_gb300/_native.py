@@ -181,6 +181,7 @@ def lib():
                                      C.c_uint64, C.POINTER(BatchLimitsC),
                                      C.POINTER(ExtendParamsC), vp, vp, C.c_uint32, vp, vp, vp]
     L.esp_int_peaks.argtypes = [vp] + [C.POINTER(C.c_double)] * 4
+    L.esp_simd16_peaks.argtypes = [vp] + [C.POINTER(C.c_double)] * 2
     L.esp_paidx_scan.argtypes = [vp, C.c_uint64, C.POINTER(PaidxInfoC), C.c_char_p, sz]
     L.esp_paidx_contigs.argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint32, vp,
                                     C.c_uint64, vp, C.c_uint64]

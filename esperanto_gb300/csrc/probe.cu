@@ -2,7 +2,8 @@
 // the DP kernels' roofline (the measured peaks cover HBM and bf16
 // only).  Each probe thread runs 8 independent dependency chains of one
 // instruction kind, long enough that issue, not latency, is the limit; the
-// result is lane-operations per second.
+// result is lane-operations per second (a 16x2 operation counts once per
+// 32-bit lane: it updates two 16-bit values).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -30,8 +31,12 @@ __global__ void __launch_bounds__(256) int_probe(uint32_t seed, uint32_t *sink) 
                 asm volatile("max.s32 %0, %0, %1;" : "+r"(x[c]) : "r"(y + c));
             } else if (KIND == 2) {  // integer add
                 asm volatile("add.u32 %0, %0, %1;" : "+r"(x[c]) : "r"(y));
-            } else {  // integer multiply-add
+            } else if (KIND == 3) {  // integer multiply-add
                 asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y | 1u), "r"(z));
+            } else if (KIND == 4) {  // 16x2 add-then-max (two 16-bit lanes)
+                x[c] = __viaddmax_s16x2(x[c], y, z + c);
+            } else {  // 16x2 three-way max
+                x[c] = __vimax3_s16x2(x[c], y, z + c);
             }
         }
     }
@@ -64,6 +69,17 @@ int run(int sms, cudaStream_t st, uint32_t *sink, double *out) {
 }
 
 }  // namespace
+
+extern "C" int esp_simd16_peaks(esp_handle *h, double *addmax, double *max3) {
+    if (!h || !addmax || !max3) return ESP_EINVAL;
+    CK(h, cudaSetDevice(h->device));
+    uint32_t *sink = nullptr;
+    CK(h, cudaMalloc((void **)&sink, 4));
+    int rc = run<4>(h->num_sms, h->stream, sink, addmax);
+    if (rc == ESP_OK) rc = run<5>(h->num_sms, h->stream, sink, max3);
+    cudaFree(sink);
+    return rc == ESP_OK ? ESP_OK : fail(h, rc, "16x2 peak probe failed");
+}
 
 extern "C" int esp_int_peaks(esp_handle *h, double *lop3, double *imnmx, double *iadd,
                              double *imad) {

@@ -565,6 +565,10 @@ int esp_server_destroy(esp_server *s);
  * integer max, integer add and integer multiply-add on the handle's GPU: the
  * denominators of the DP kernels' integer roofline.  Runs a few milliseconds of probes. */
 int esp_int_peaks(esp_handle *h, double *lop3, double *imnmx, double *iadd, double *imad);
+/* The same for the 16x2 SIMD add-then-max and three-way max the two-pairs-
+ * per-thread DP kernel is built on (per 32-bit lane; each updates two 16-bit
+ * values). */
+int esp_simd16_peaks(esp_handle *h, double *addmax, double *max3);
 
 /* ---- allocation-free variant (no counterpart in the reference) ----
  *
