@@ -49,7 +49,9 @@ MYERS_OPS_PER_CELL = 10.0 / 32.0
 # per DP cell, captured on a
 # 524,288-pair case of the same distribution and scaled by cells.
 TRAFFIC_BYTES = {0: 50.3e6 + 348.3e6, 1: 125.5e6 + 9.3e6}
-TRAFFIC_PER_CELL = {2: (2713001472 + 6431804160) / 7716062109}
+# keyed by (workload, SIMD lanes): one pair per thread, two pairs per thread
+TRAFFIC_PER_CELL = {(2, 1): (2713001472 + 6431804160) / 7716062109,
+                    (2, 2): (10934568e3 + 16413622e3) / 15444885371}
 TRAFFIC_SOURCE = {0: "profiles/gotoh_kernel_config0_65536pairs.md",
                   1: "profiles/myers_kernel_config1_1048576pairs.md",
                   2: "profiles/gotoh_kernel_traffic_config2.md (scaled by cells)"}
@@ -607,8 +609,8 @@ def main():
     traffic = None
     if config in TRAFFIC_BYTES and n_pairs == DEFAULT_PAIRS[config]:
         traffic = TRAFFIC_BYTES[config]
-    elif config in TRAFFIC_PER_CELL:
-        traffic = TRAFFIC_PER_CELL[config] * wl.cells
+    elif (config, lanes) in TRAFFIC_PER_CELL:
+        traffic = TRAFFIC_PER_CELL[(config, lanes)] * wl.cells
     plain = None
     if hasattr(wl, "plain_per_call"):
         pps, sample = wl.plain_per_call(seed, 2000, buf)
