@@ -174,22 +174,39 @@ int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
                          const esp_n_interval *n_iv, uint64_t n_iv_count,
                          esp_myers_result *out) {
     if (!h || !out || (n_pairs && (!pairs || !arena))) return fail(h, ESP_EINVAL, "null argument");
-    // longest read (sizes the kernel's limb count); large batches are
-    // scanned by several host threads
+    // Large batches run as a pipeline of chunks: the inputs of chunk c+1 and
+    // the results of chunk c-1 cross the host link while chunk c computes.
+    const uint64_t C = n_pairs >= (1u << 18) ? 4 : 1;
+    std::vector<uint64_t> bounds(C + 1);
+    for (uint64_t c = 0; c <= C; c++) bounds[c] = n_pairs * c / C;
+    // longest read (sizes the kernel's limb count) and the arena prefix each
+    // chunk reads; large batches are scanned on the host pool
     uint32_t mx = 1;
+    std::vector<uint64_t> arena_end(C, 0);  // bases
     {
         unsigned T = n_pairs < (1u << 16) ? 1 : (unsigned)std::min<uint64_t>(16, n_pairs >> 15);
         if (T > 1) T = std::min(T, host_pool(h).size());
         std::vector<uint32_t> part(T, 1);
+        std::vector<uint64_t> ends(T * C, 0);
         auto work = [&](unsigned t) {
             uint32_t m = 1;
-            for (uint64_t k = n_pairs * t / T, e = n_pairs * (t + 1) / T; k < e; k++)
-                m = std::max(m, pairs[k].read_len);
+            for (uint64_t c = 0; c < C; c++) {
+                const uint64_t a = bounds[c], len = bounds[c + 1] - a;
+                uint64_t e = 0;
+                for (uint64_t k = a + len * t / T, z = a + len * (t + 1) / T; k < z; k++) {
+                    const esp_myers_pair &P = pairs[k];
+                    m = std::max(m, P.read_len);
+                    e = std::max({e, P.read_pos + P.read_len, P.text_pos + P.text_len});
+                }
+                ends[t * C + c] = e;
+            }
             part[t] = m;
         };
         if (T > 1) host_pool(h).run(T, work);
         else work(0);
         for (uint32_t m : part) mx = std::max(mx, m);
+        for (unsigned t = 0; t < T; t++)
+            for (uint64_t c = 0; c < C; c++) arena_end[c] = std::max(arena_end[c], ends[t * C + c]);
     }
     if (mx > (uint32_t)LONG_MAX_M) return fail(h, ESP_EINVAL, "Myers read length must be <= 256");
     CK(h, cudaSetDevice(h->device));
@@ -201,20 +218,67 @@ int esp_batch_myers_host(esp_handle *h, int mode, const esp_myers_pair *pairs,
     if ((rc = grow_device(h, &h->d_bat, &h->d_bat_cap, sz_p + sz_iv + sz_a + sz_o)) != ESP_OK)
         return rc;
     uint8_t *b = (uint8_t *)h->d_bat;
-    cudaStream_t st = h->stream;
-    CK(h, cudaMemcpyAsync(b, pairs, n_pairs * sizeof(esp_myers_pair), cudaMemcpyHostToDevice, st));
-    if (n_iv_count)
-        CK(h, cudaMemcpyAsync(b + sz_p, n_iv, n_iv_count * sizeof(esp_n_interval),
-                              cudaMemcpyHostToDevice, st));
-    CK(h, cudaMemcpyAsync(b + sz_p + sz_iv, arena, arena_bytes, cudaMemcpyHostToDevice, st));
-    CK(h, cudaMemsetAsync(b + sz_p + sz_iv + arena_bytes, 0, 16, st));
+    esp_myers_pair *dp = (esp_myers_pair *)b;
+    const esp_n_interval *div = (const esp_n_interval *)(b + sz_p);
+    uint8_t *da = b + sz_p + sz_iv;
     esp_myers_result *dout = (esp_myers_result *)(b + sz_p + sz_iv + sz_a);
-    rc = esp_batch_myers_device(h, mode, (const esp_myers_pair *)b, n_pairs, mx,
-                                b + sz_p + sz_iv, arena_bytes,
-                                (const esp_n_interval *)(b + sz_p), n_iv_count, dout, st);
-    if (rc != ESP_OK) return rc;
-    CK(h, cudaMemcpyAsync(out, dout, n_pairs * sizeof(esp_myers_result), cudaMemcpyDeviceToHost, st));
+    cudaStream_t st = h->stream;
+    if (C == 1) {
+        CK(h, cudaMemcpyAsync(dp, pairs, n_pairs * sizeof(esp_myers_pair), cudaMemcpyHostToDevice, st));
+        if (n_iv_count)
+            CK(h, cudaMemcpyAsync((void *)div, n_iv, n_iv_count * sizeof(esp_n_interval),
+                                  cudaMemcpyHostToDevice, st));
+        CK(h, cudaMemcpyAsync(da, arena, arena_bytes, cudaMemcpyHostToDevice, st));
+        CK(h, cudaMemsetAsync(da + arena_bytes, 0, 16, st));
+        rc = esp_batch_myers_device(h, mode, dp, n_pairs, mx, da, arena_bytes, div, n_iv_count,
+                                    dout, st);
+        if (rc != ESP_OK) return rc;
+        CK(h, cudaMemcpyAsync(out, dout, n_pairs * sizeof(esp_myers_result), cudaMemcpyDeviceToHost, st));
+        CK(h, cudaStreamSynchronize(st));
+        return ESP_OK;
+    }
+    if (!h->copy_stream) CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    cudaStream_t cs = h->copy_stream;
+    std::vector<cudaEvent_t> ev(2 * C);
+    for (auto &e : ev) CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    auto release = [&] {
+        for (auto &e : ev) cudaEventDestroy(e);
+    };
+    // inputs, chunk by chunk: the pairs and the arena prefix the chunk reads
+    // (the last chunk also gets the zero tail that 64-bit code loads read)
+    if (n_iv_count)
+        CK(h, cudaMemcpyAsync((void *)div, n_iv, n_iv_count * sizeof(esp_n_interval),
+                              cudaMemcpyHostToDevice, cs));
+    uint64_t copied = 0;  // arena bytes already sent
+    for (uint64_t c = 0; c < C; c++) {
+        const uint64_t a = bounds[c], n = bounds[c + 1] - a;
+        CK(h, cudaMemcpyAsync(dp + a, pairs + a, n * sizeof(esp_myers_pair), cudaMemcpyHostToDevice, cs));
+        uint64_t need = c + 1 == C ? arena_bytes
+                                   : std::min<uint64_t>(arena_bytes, (arena_end[c] + 3) / 4 + 16);
+        if (need > copied) {
+            CK(h, cudaMemcpyAsync(da + copied, arena + copied, need - copied, cudaMemcpyHostToDevice, cs));
+            copied = need;
+        }
+        if (c + 1 == C) CK(h, cudaMemsetAsync(da + arena_bytes, 0, 16, cs));
+        CK(h, cudaEventRecord(ev[c], cs));
+    }
+    for (uint64_t c = 0; c < C; c++) {
+        const uint64_t a = bounds[c], n = bounds[c + 1] - a;
+        CK(h, cudaStreamWaitEvent(st, ev[c], 0));
+        rc = esp_batch_myers_device(h, mode, dp + a, n, mx, da, arena_bytes, div, n_iv_count,
+                                    dout + a, st);
+        if (rc != ESP_OK) {
+            release();
+            return rc;
+        }
+        CK(h, cudaEventRecord(ev[C + c], st));
+        CK(h, cudaStreamWaitEvent(cs, ev[C + c], 0));
+        CK(h, cudaMemcpyAsync(out + a, dout + a, n * sizeof(esp_myers_result), cudaMemcpyDeviceToHost, cs));
+    }
+    CK(h, cudaStreamSynchronize(cs));
     CK(h, cudaStreamSynchronize(st));
+    release();
+    h->launches = (int)C;
     return ESP_OK;
 }
 

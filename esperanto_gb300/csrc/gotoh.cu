@@ -1049,7 +1049,8 @@ __device__ __forceinline__ void dp_column2(Strip2 &S, const uint32_t oe1, const 
 template <int MASK, bool CHECK>
 __device__ __forceinline__ void dp_cols2(Strip2 &S, const uint32_t oe1, const uint32_t oe4,
                                          const uint32_t ex4, int a, int b, uint32_t &diag,
-                                         const Seq &winA, const Seq &winB, uint2 *rb, int plo,
+                                         const uint8_t *warena, uint64_t wposA, uint64_t wposB,
+                                         uint2 *rb, int plo,
                                          int phi, int lo7, uint32_t *tbA, uint32_t *tbB) {
     uint2 *rbr = rb + (size_t)(a - plo) * 32;
     uint2 wn0 = make_uint2(0u, 0u), wn1 = make_uint2(0u, 0u);
@@ -1058,8 +1059,8 @@ __device__ __forceinline__ void dp_cols2(Strip2 &S, const uint32_t oe1, const ui
         if (a + 1 <= b) wn1 = rbr[32];
     }
     for (int j = a; j <= b;) {
-        uint32_t cwA = load16(winA.arena, winA.pos + (uint64_t)(j - 1));
-        uint32_t cwB = load16(winB.arena, winB.pos + (uint64_t)(j - 1));
+        uint32_t cwA = load16(warena, wposA + (uint64_t)(j - 1));
+        uint32_t cwB = load16(warena, wposB + (uint64_t)(j - 1));
         int cnt = min(16, b - j + 1);
 #pragma unroll 1
         for (int k = 0; k < cnt; k++, j++) {
@@ -1095,8 +1096,8 @@ __device__ __forceinline__ void dp_cols2(Strip2 &S, const uint32_t oe1, const ui
 
 // Fill the DP of two pairs with identical geometry (shared g, m, n, sw).
 __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut, int m, int n,
-                         const Geo &g, const Seq &readA, const Seq &readB, const Seq &winA,
-                         const Seq &winB, uint32_t *tbA, uint32_t *tbB, int sw, uint2 *rb,
+                         const Geo &g, const Seq &readA, const Seq &readB, const uint8_t *warena,
+                         uint64_t wposA, uint64_t wposB, uint32_t *tbA, uint32_t *tbB, int sw, uint2 *rb,
                          FillResult &FA, FillResult &FB) {
     const uint32_t oe1 = (uint32_t)(K.oe1 & 0xffff) * 0x10001u;
     const uint32_t oe4 = (uint32_t)(K.oe4 & 0xffff) * 0x10001u;
@@ -1125,7 +1126,7 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
         int lo7 = (int)(S.lohi[STRIP - 1] & 0xffffu);
         int hi0 = (int)(S.lohi[0] >> 16);
         uint32_t rwA = load16(readA.arena, readA.pos + (uint64_t)(i0 - 1));
-        uint32_t rwB = load16(readB.arena, readB.pos + (uint64_t)(i0 - 1));
+        uint32_t rwB = load16(readA.arena, readB.pos + (uint64_t)(i0 - 1));  // one arena
         uint32_t rnA = readA.cnt ? nmask16(readA.iv, readA.cnt, i0 - 1) : 0u;
         uint32_t rnB = readB.cnt ? nmask16(readB.iv, readB.cnt, i0 - 1) : 0u;
 #pragma unroll
@@ -1140,11 +1141,11 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
         if (clo - 1 >= plo && clo - 1 <= phi) diag = rb[(size_t)(clo - 1 - plo) * 32].x;
         uint32_t *ta = tbA + (size_t)s * sw * 32, *tbq = tbB + (size_t)s * sw * 32;
         int a_end = min(lo7, chi);
-        dp_cols2<1, true>(S, oe1, oe4, ex4, clo, a_end, diag, winA, winB, rb, plo, phi, lo7, ta,
+        dp_cols2<1, true>(S, oe1, oe4, ex4, clo, a_end, diag, warena, wposA, wposB, rb, plo, phi, lo7, ta,
                           tbq);
         int b_beg = lo7 + 1, b_end = min(hi0 - 1, chi);
         if (b_beg <= b_end)
-            dp_cols2<0, false>(S, oe1, oe4, ex4, b_beg, b_end, diag, winA, winB, rb, plo, phi,
+            dp_cols2<0, false>(S, oe1, oe4, ex4, b_beg, b_end, diag, warena, wposA, wposB, rb, plo, phi,
                                lo7, ta + (size_t)(b_beg - clo) * 32,
                                tbq + (size_t)(b_beg - clo) * 32);
         int c_beg = max(lo7 + 1, hi0);
@@ -1153,7 +1154,7 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
         for (int r = 0; r < STRIP; r++)
             S.lohi[r] = (uint32_t)g.lo(i0 + r) | ((uint32_t)g.hi(i0 + r) << 16);
         if (c_beg <= chi)
-            dp_cols2<1, true>(S, oe1, oe4, ex4, c_beg, chi, diag, winA, winB, rb, plo, phi, lo7,
+            dp_cols2<1, true>(S, oe1, oe4, ex4, c_beg, chi, diag, warena, wposA, wposB, rb, plo, phi, lo7,
                               ta + (size_t)(c_beg - clo) * 32, tbq + (size_t)(c_beg - clo) * 32);
         // row bookkeeping in row order (extend.rs:795-827), per lane
 #pragma unroll
@@ -1197,7 +1198,7 @@ __device__ __noinline__ void fill2_call(const GotohConst &K, const uint32_t *__r
                                         const PairSetup &A, const PairSetup &B, uint32_t *tbA,
                                         uint32_t *tbB, uint32_t *rb, FillResult &FA,
                                         FillResult &FB) {
-    dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win, B.win, tbA, tbB, A.sw,
+    dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win.arena, A.win.pos, B.win.pos, tbA, tbB, A.sw,
              reinterpret_cast<uint2 *>(rb), FA, FB);
 }
 

@@ -105,3 +105,24 @@ def test_config1_subset():
     got = B.myers_batch_host(pairs, arena)
     want = _oracle_batch(arena, pairs, None, B.MYERS_BEST_END)
     assert [(int(g["dist"]), int(g["pos"])) for g in got] == want
+
+
+def test_host_batch_pipeline_chunks():
+    """Host batches of 2^18 pairs and more run as four chunks whose copies
+    overlap the neighbouring chunks' kernels: the results equal those of
+    unchunked calls on the same pairs, also when the pairs reference the
+    arena out of order (each chunk then needs most of the arena), and the
+    oracle on a sample."""
+    arena, pairs = B.synth_myers(5, 300000)
+    rng = np.random.default_rng(3)
+    for order in (np.arange(len(pairs)), rng.permutation(len(pairs))):
+        p = pairs[order]
+        got = B.myers_batch_host(p, arena)
+        half = len(p) // 2  # below the chunking size: one launch each
+        want = np.concatenate([B.myers_batch_host(p[:half], arena),
+                               B.myers_batch_host(p[half:], arena)])
+        assert (got == want).all()
+    sample = [int(k) for k in rng.choice(len(pairs), 300, replace=False)]
+    got = B.myers_batch_host(pairs, arena)
+    want = _oracle_batch(arena, pairs[sample], None, B.MYERS_BEST_END)
+    assert [(int(got[k]["dist"]), int(got[k]["pos"])) for k in sample] == want
