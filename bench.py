@@ -206,6 +206,9 @@ class GotohWorkload(Workload):
         if self.lanes == 2:
             self.dtype = "int16x2"
 
+        self._arena_bytes = arena.nbytes
+        self._pairs = pairs
+
         def step():
             buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
                                                 d_arena.data_ptr(), arena.nbytes, None, 0,
@@ -261,6 +264,40 @@ class GotohWorkload(Workload):
             one(c)
         dt = time.perf_counter() - t
         return sample / dt, f"{sample} pairs of the same workload, one esp_run_band call each"
+
+    def hint_measure(self, buf, torch, stream, steps=5):
+        """extend_hint (extend.rs:392-428) over the same resident batch: the
+        banded attempt, escalating to the full matrix on a touch or a low
+        score.  Returns GCUPS (cells of both attempts), ms per call and the
+        escalation rate."""
+        from esperanto_gb300 import _native as N
+        from esperanto_gb300 import batch as B
+        L = N.lib()
+        d_arena, d_pairs, d_out, d_cig, lim, p = self._keep
+        hlim = N.BatchLimitsC(lim.max_read_len, lim.max_win_len, 30)
+
+        def call():
+            buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_HINT, d_pairs.data_ptr(),
+                                                self.n, d_arena.data_ptr(), self._arena_bytes,
+                                                None, 0, C.byref(hlim), C.byref(p),
+                                                d_out.data_ptr(), d_cig.data_ptr(), self.stride,
+                                                None))
+        for _ in range(3):
+            call()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)  # the handle's stream, where the kernels run
+        for _ in range(steps):
+            call()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / steps
+        out = d_out.cpu().numpy().view(B.EXT_DTYPE)
+        esc = out["escalated"]
+        cells = B.cells_of(self._pairs, B.MODE_HINT, esc)
+        return {"gcups": cells / (ms / 1e3) / 1e9, "ms_per_call": ms,
+                "escalation_rate": float(esc.mean()), "cells_per_call": int(cells),
+                "bad_status": int((out["status"] != 0).sum())}
 
     def cpu_reference(self, seed, sample, threads):
         import oracle as O
@@ -666,6 +703,10 @@ def main():
     if config == 3:
         line["config"]["candidates"] = wl.n_cands
         line["config"]["rescued"] = wl.found
+    if config == 0:
+        # the same pairs through extend_hint: its escalation rate is the
+        # measure of how often the reference's two-attempt policy runs twice
+        line["extend_hint"] = wl.hint_measure(buf, torch, stream)
     print(json.dumps(line), flush=True)
 
 

@@ -15,7 +15,7 @@ if not torch.cuda.is_available():
 
 import esperanto_gb300 as E  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
-from gpu_helpers import compare, kernel_buffer  # noqa: E402
+from gpu_helpers import _compare, compare, kernel_buffer  # noqa: E402
 
 
 def _gpu_kind(kind, case):
@@ -262,6 +262,10 @@ def test_paired_kernel_geometry_groups():
     cases, ctx = _geometry_groups(5, groups, 37)
     dirs = [k % 3 for k in range(len(cases))]
     assert compare(cases, dirs, ctxs=ctx, kernels=("paired",)) == len(cases)
+    # extend_hint batches on a handle set to a paired variant run the
+    # one-pair kernel (hint offsets differ per pair) with the same results
+    hint = [(r, w, (band[0] if band else 0, 30)) for r, w, band in cases[:200]]
+    assert _compare(hint, dirs[:200], B.MODE_HINT, None, "paired") == 200
 
 
 def test_paired_kernel_variants_on_mixed_batch():
@@ -314,3 +318,21 @@ def test_autotune_per_length_class():
         cig = d_cig.cpu().numpy().view(np.uint32).reshape(n, 32)
         for k in range(0, n, 101):
             assert (cig[k, :out[k]["n_ops"]] == wc[k, :out[k]["n_ops"]]).all()
+
+
+def test_hint_escalation_decisions_match_oracle():
+    """extend_hint's second attempt (extend.rs:392-428: a touch or a low score
+    escalates to the full matrix) runs for exactly the pairs the oracle
+    escalates, on the banded and the mixed-length workloads; the escalation
+    rate is then the oracle's too."""
+    from gpu_helpers import gpu_batch
+    for shape, n in ((0, 1024), (2, 512)):
+        arena, pairs = B.synth_gotoh(7, n, shape)
+        cases = []
+        for k in range(n):
+            r, w = B.decode_pair(arena, pairs[k])
+            cases.append((r, w, (int(pairs[k]["band_offset"]), 30)))
+        got = gpu_batch(cases, 0, B.MODE_HINT)
+        for k, (r, w, band) in enumerate(cases):
+            want, esc = O.extend_hint(r, w, O.Params(), offset=band[0], with_escalation=True)
+            assert got[k][0] == want.key() and got[k][2] == esc, (shape, k)
