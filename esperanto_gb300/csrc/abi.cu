@@ -21,6 +21,26 @@ static int default_variant() {
     return 1;
 }
 
+// Kernel variant of a hint-mode batch of n pairs.  Hint batches repeat one
+// geometry when their windows are cut the same way (the splice flanks: read
+// segment vs segment + 30 bases at offset 0), so from 2^20 pairs on they run
+// the paired kernel (measured: the 69M-pair splice flank batch 1,063 vs 974
+// GCUPS); smaller ones cannot fill the GPU with two-pair items (a 65,536-pair
+// batch 3.94 vs 3.14 ms, the serve loop's requests 16.0 vs 22.5 M pairs/s
+// peak) and run one pair per thread.  ESP_GOTOH_HINT_VARIANT (0..3)
+// overrides.
+static int hint_variant(esp_handle *h, uint64_t n) {
+    if (h->hint_variant < -1) {
+        const char *v = getenv("ESP_GOTOH_HINT_VARIANT");
+        h->hint_variant =
+            (v && v[0] >= '0' && v[0] < '0' + esp::kGotohVariants && !v[1]) ? v[0] - '0' : -1;
+    }
+    if (h->hint_variant >= 0) return h->hint_variant;
+    if (h->binning && n >= (1u << 20)) return 3;
+    if (h->variant < 0) h->variant = default_variant();
+    return esp::gotoh_paired(h->variant) ? h->variant - 2 : h->variant;
+}
+
 // Whether band-mode batches of this handle run a paired kernel (set, or
 // chosen by autotuning for any length class).
 static bool band_paired(esp_handle *h, int mode) {
@@ -99,11 +119,11 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
     if (h->variant < 0) h->variant = default_variant();
     // the paired kernels need neighbours of the binned list with one band
-    // geometry: band mode only (hint offsets differ per pair)
+    // geometry
     auto usable = [&](int v) {
         return esp::gotoh_paired(v) && (mode != ESP_MODE_BAND || !h->binning) ? v - 2 : v;
     };
-    int var = usable(h->variant);
+    int var = mode == ESP_MODE_HINT ? hint_variant(h, n_pairs) : usable(h->variant);
     // autotuned handle: one variant for every class runs as a single launch
     bool tuned_split = false;
     if (h->tuned && mode == ESP_MODE_BAND) {
@@ -509,7 +529,9 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     // items of a chunk outlast the chunk's other work (measured on the mixed
     // workload: 1M pairs at 21.3 ms paired vs 17.9 ms one per thread, 4M at
     // 64.4 vs 71.5) and the chunk tails cost more than the copies they hide.
-    const uint64_t C = n_pairs >= (1u << 20) && !band_paired(h, mode) ? 4 : 1;
+    const bool paired = mode == ESP_MODE_BAND ? band_paired(h, mode)
+                                              : esp::gotoh_paired(hint_variant(h, n_pairs));
+    const uint64_t C = n_pairs >= (1u << 20) && !paired ? 4 : 1;
     std::vector<uint64_t> bounds(C + 1);
     for (uint64_t c = 0; c <= C; c++) bounds[c] = n_pairs * c / C;
     std::vector<ScanOut> sc;
