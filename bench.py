@@ -432,6 +432,13 @@ class SpliceWorkload(Workload):
         self.d2h = out_pin.nbytes + cig_pin.nbytes
         self.input_mb = (garena.nbytes + rarena.nbytes) / 1e6
         self.n_cands = len(cands)
+        # the flank DPs (22 extend_hint pairs per candidate) run as one hint
+        # batch: on the 16x2 paired kernel from 2^20 pairs unless overridden
+        forced = os.environ.get("ESP_GOTOH_HINT_VARIANT")
+        paired = int(forced) >= 2 if forced else 22 * len(cands) >= (1 << 20)
+        self.lanes = 2 if paired else 1
+        if paired:
+            self.dtype = "int16x2"
 
     def cpu_reference(self, seed, sample, threads):
         import oracle as O
