@@ -199,8 +199,9 @@ class GotohWorkload(Workload):
                              "ms": [[round(ms[nv * s + v], 3) for v in range(nv)]
                                     for s in range(5)]}
             chosen = list(variants)
-        else:
-            chosen = [int(os.environ.get("ESP_GOTOH_VARIANT", "1"))]
+        else:  # the handle's default: by size unless ESP_GOTOH_VARIANT is set
+            forced = os.environ.get("ESP_GOTOH_VARIANT")
+            chosen = [int(forced) if forced else (3 if n >= (1 << 20) else 1)]
         # variants 2 / 3 compute two pairs per thread in 16-bit SIMD halves
         self.lanes = 2 if any(v >= 2 for v in chosen) else 1
         if self.lanes == 2:

@@ -14,11 +14,28 @@
 #include "esp_host.h"
 
 // Kernel variant of a handle that was neither set nor tuned: the
-// ESP_GOTOH_VARIANT environment variable (0..3), else 1.
-static int default_variant() {
+// ESP_GOTOH_VARIANT environment variable (0..3), else 1 -- and then band
+// batches of 2^20 pairs and more take the paired kernel (band_variant).
+static int default_variant(bool *by_size = nullptr) {
     const char *v = getenv("ESP_GOTOH_VARIANT");
-    if (v && v[0] >= '0' && v[0] < '0' + esp::kGotohVariants && !v[1]) return v[0] - '0';
-    return 1;
+    const bool env = v && v[0] >= '0' && v[0] < '0' + esp::kGotohVariants && !v[1];
+    if (by_size) *by_size = !env;
+    return env ? v[0] - '0' : 1;
+}
+
+static void resolve_variant(esp_handle *h) {
+    if (h->variant < 0) h->variant = default_variant(&h->variant_by_size);
+}
+
+// Variant of an untuned band batch of n pairs: the handle's, except that a
+// handle left at the default runs batches of 2^20 pairs and more on the
+// paired kernel (the mixed-length workload: 1,054 vs ~900 GCUPS at 2^20
+// pairs, 1,148 vs 930 at 2^22; at 2^18 the one-pair kernel wins, 738 vs
+// 397).  esp_batch_autotune measures instead of assuming.
+static int band_variant(esp_handle *h, uint64_t n) {
+    resolve_variant(h);
+    if (h->variant_by_size && h->binning && n >= (1u << 20)) return 3;
+    return h->variant;
 }
 
 // Kernel variant of a hint-mode batch of n pairs.  Hint batches repeat one
@@ -37,20 +54,20 @@ static int hint_variant(esp_handle *h, uint64_t n) {
     }
     if (h->hint_variant >= 0) return h->hint_variant;
     if (h->binning && n >= (1u << 20)) return 3;
-    if (h->variant < 0) h->variant = default_variant();
+    resolve_variant(h);
     return esp::gotoh_paired(h->variant) ? h->variant - 2 : h->variant;
 }
 
-// Whether band-mode batches of this handle run a paired kernel (set, or
+// Whether a band batch of n pairs runs a paired kernel (set, by size, or
 // chosen by autotuning for any length class).
-static bool band_paired(esp_handle *h, int mode) {
-    if (mode != ESP_MODE_BAND || !h->binning) return false;
+static bool band_paired(esp_handle *h, uint64_t n) {
+    if (!h->binning) return false;
     if (h->tuned) {
         for (int s = 0; s < esp::kLengthClasses; s++)
             if (esp::gotoh_paired(h->tune[s])) return true;
         return false;
     }
-    return esp::gotoh_paired(h->variant < 0 ? default_variant() : h->variant);
+    return esp::gotoh_paired(band_variant(h, n));
 }
 
 // Enqueue the DP launches of one batch whose inputs are on the device.
@@ -117,13 +134,13 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
     uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
     uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    if (h->variant < 0) h->variant = default_variant();
+    resolve_variant(h);
     // the paired kernels need neighbours of the binned list with one band
     // geometry
     auto usable = [&](int v) {
         return esp::gotoh_paired(v) && (mode != ESP_MODE_BAND || !h->binning) ? v - 2 : v;
     };
-    int var = mode == ESP_MODE_HINT ? hint_variant(h, n_pairs) : usable(h->variant);
+    int var = mode == ESP_MODE_HINT ? hint_variant(h, n_pairs) : usable(band_variant(h, n_pairs));
     // autotuned handle: one variant for every class runs as a single launch
     bool tuned_split = false;
     if (h->tuned && mode == ESP_MODE_BAND) {
@@ -258,7 +275,7 @@ int reserve_dp(esp_handle *h, uint64_t max_pairs, uint32_t max_m, uint32_t max_n
     add_limits(L2, max_m, max_n, -1);
     uint64_t tbw = std::max(L1.tb_words, L2.tb_words), rbw = std::max(L1.rb_words, L2.rb_words);
     uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    if (h->variant < 0) h->variant = default_variant();
+    resolve_variant(h);
     if (h->gotoh_bps[h->variant] == 0)
         h->gotoh_bps[h->variant] = esp::gotoh_blocks_per_sm(128, h->variant);
     const uint64_t slot_pairs = esp::gotoh_paired(h->variant) ? 2 : 1;
@@ -306,6 +323,7 @@ int esp_set_warp_max(esp_handle *h, long warp_max) {
 int esp_set_kernel_variant(esp_handle *h, int variant) {
     if (!h || variant < -1 || variant >= esp::kGotohVariants) return ESP_EINVAL;
     h->variant = variant;
+    h->variant_by_size = false;  // a -1 is resolved again at the next batch
     h->tuned = false;
     for (int s = 0; s < esp::kLengthClasses; s++) h->tune[s] = -1;
     return ESP_OK;
@@ -529,7 +547,7 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     // items of a chunk outlast the chunk's other work (measured on the mixed
     // workload: 1M pairs at 21.3 ms paired vs 17.9 ms one per thread, 4M at
     // 64.4 vs 71.5) and the chunk tails cost more than the copies they hide.
-    const bool paired = mode == ESP_MODE_BAND ? band_paired(h, mode)
+    const bool paired = mode == ESP_MODE_BAND ? band_paired(h, n_pairs)
                                               : esp::gotoh_paired(hint_variant(h, n_pairs));
     const uint64_t C = n_pairs >= (1u << 20) && !paired ? 4 : 1;
     std::vector<uint64_t> bounds(C + 1);

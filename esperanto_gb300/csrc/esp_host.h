@@ -26,6 +26,7 @@ struct esp_handle {
     uint64_t launches = 0;
     int gotoh_bps[esp::kGotohVariants] = {};  // resident DP blocks per SM (queried once)
     int variant = -1;   // DP kernel variant; -1 = ESP_GOTOH_VARIANT env or default
+    bool variant_by_size = false;  // default variant: large band batches run paired
     int hint_variant = -2;  // variant of hint-mode batches: >= 0 forced (ESP_GOTOH_HINT_VARIANT),
                             // -1 by batch size (abi.cu hint_variant), -2 = env not read yet
     long warp_max = -1; // batches of at most this many pairs run warp-per-pair; -1 = ESP_WARP_MAX or 2048

@@ -96,10 +96,10 @@ int esp_set_warp_max(esp_handle *h, long warp_max);
  * reference): 0 = one pair per thread at 3 resident blocks per SM, 1 = at 4
  * blocks, 2 / 3 = two pairs of identical band geometry per thread (16x2 SIMD
  * lanes) at 3 / 4 blocks; -1 = the ESP_GOTOH_VARIANT environment variable,
- * else 1.  Applies to band-mode batches and clears a previous autotuning.
- * Hint-mode batches choose by size: variant 3 from 2^20 pairs on, else the
- * one-pair variant (ESP_GOTOH_HINT_VARIANT overrides).  All variants give
- * identical results. */
+ * else by size: variant 3 for batches of 2^20 pairs and more, 1 below.
+ * Applies to band-mode batches and clears a previous autotuning.  Hint-mode
+ * batches choose by size the same way (ESP_GOTOH_HINT_VARIANT overrides).
+ * All variants give identical results. */
 int esp_set_kernel_variant(esp_handle *h, int variant);
 int esp_destroy(esp_handle *h);
 /* Message of the last error on this handle (static storage of the handle). */

@@ -338,25 +338,25 @@ def test_hint_escalation_decisions_match_oracle():
             assert got[k][0] == want.key() and got[k][2] == esc, (shape, k)
 
 
-def test_large_hint_batch_runs_paired_kernel_with_same_results():
-    """Hint batches of 2^20 pairs and more run the two-pairs-per-thread
-    kernel (both attempts); the results equal the one-pair kernel's (a handle
-    forced to it with ESP_GOTOH_HINT_VARIANT=1) and the oracle's on a
-    sample."""
+def test_large_batches_run_paired_kernel_with_same_results():
+    """Band and hint batches of 2^20 pairs and more on a default handle run
+    the two-pairs-per-thread kernel; the results equal the one-pair kernel's
+    (handles forced to it by ESP_GOTOH_VARIANT / ESP_GOTOH_HINT_VARIANT) and,
+    for hint batches, the oracle's on a sample."""
     import os
     from esperanto_gb300.extend import ExtendBuffer
     arena, pairs = B.synth_gotoh(13, 1 << 20, 0)
-    big = B.extend_batch_host(pairs, arena, mode=B.MODE_HINT, cigar_stride=32,
-                              buf=ExtendBuffer())
-    os.environ["ESP_GOTOH_HINT_VARIANT"] = "1"
-    try:
-        one = B.extend_batch_host(pairs, arena, mode=B.MODE_HINT, cigar_stride=32,
-                                  buf=ExtendBuffer())
-    finally:
-        del os.environ["ESP_GOTOH_HINT_VARIANT"]
-    assert (big[0] == one[0]).all()
-    used = np.arange(32)[None, :] < np.minimum(big[0]["n_ops"], 32)[:, None]
-    assert ((big[1] == one[1]) | ~used).all()
+    for mode, env in ((B.MODE_BAND, "ESP_GOTOH_VARIANT"), (B.MODE_HINT, "ESP_GOTOH_HINT_VARIANT")):
+        big = B.extend_batch_host(pairs, arena, mode=mode, cigar_stride=32, buf=ExtendBuffer())
+        os.environ[env] = "1"
+        try:
+            one = B.extend_batch_host(pairs, arena, mode=mode, cigar_stride=32,
+                                      buf=ExtendBuffer())
+        finally:
+            del os.environ[env]
+        assert (big[0] == one[0]).all()
+        used = np.arange(32)[None, :] < np.minimum(big[0]["n_ops"], 32)[:, None]
+        assert ((big[1] == one[1]) | ~used).all()
     rng = np.random.default_rng(1)
     for k in rng.choice(len(pairs), 200, replace=False):
         r, w = B.decode_pair(arena, pairs[k])
