@@ -543,13 +543,14 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     CK(h, cudaSetDevice(h->device));
     // Large batches run as a pipeline of chunks: the inputs of chunk c+1 and
     // the results of chunk c-1 cross the host link while chunk c computes.
-    // Not for the paired kernels: an item holds two pairs, so the longest
-    // items of a chunk outlast the chunk's other work (measured on the mixed
-    // workload: 1M pairs at 21.3 ms paired vs 17.9 ms one per thread, 4M at
-    // 64.4 vs 71.5) and the chunk tails cost more than the copies they hide.
+    // The paired kernels take two chunks, not four: an item holds two pairs,
+    // so a chunk's longest items outlast its other work and smaller chunks
+    // cost more in tails than their copies hide (mixed workload, 4M pairs:
+    // 59.3 ms end to end in two chunks, 61.7 in one; 1M-pair launches at
+    // 14.6 ms against 54.5 ms for 4M).
     const bool paired = mode == ESP_MODE_BAND ? band_paired(h, n_pairs)
                                               : esp::gotoh_paired(hint_variant(h, n_pairs));
-    const uint64_t C = n_pairs >= (1u << 20) && !paired ? 4 : 1;
+    const uint64_t C = paired ? (n_pairs >= (1u << 21) ? 2 : 1) : (n_pairs >= (1u << 20) ? 4 : 1);
     std::vector<uint64_t> bounds(C + 1);
     for (uint64_t c = 0; c <= C; c++) bounds[c] = n_pairs * c / C;
     std::vector<ScanOut> sc;
