@@ -340,13 +340,15 @@ def test_hint_escalation_decisions_match_oracle():
 
 def test_large_batches_run_paired_kernel_with_same_results():
     """Band and hint batches of 2^20 pairs and more on a default handle run
-    the two-pairs-per-thread kernel; the results equal the one-pair kernel's
-    (handles forced to it by ESP_GOTOH_VARIANT / ESP_GOTOH_HINT_VARIANT) and,
-    for hint batches, the oracle's on a sample."""
+    the two-pairs-per-thread kernel (2^21 band pairs: as the host pipeline's
+    two chunks); the results equal the one-pair kernel's (handles forced to
+    it by ESP_GOTOH_VARIANT / ESP_GOTOH_HINT_VARIANT; 2^21 pairs: four
+    chunks) and, for hint batches, the oracle's on a sample."""
     import os
     from esperanto_gb300.extend import ExtendBuffer
-    arena, pairs = B.synth_gotoh(13, 1 << 20, 0)
-    for mode, env in ((B.MODE_BAND, "ESP_GOTOH_VARIANT"), (B.MODE_HINT, "ESP_GOTOH_HINT_VARIANT")):
+    for mode, env, n in ((B.MODE_BAND, "ESP_GOTOH_VARIANT", 1 << 21),
+                         (B.MODE_HINT, "ESP_GOTOH_HINT_VARIANT", 1 << 20)):
+        arena, pairs = B.synth_gotoh(13, n, 0)
         big = B.extend_batch_host(pairs, arena, mode=mode, cigar_stride=32, buf=ExtendBuffer())
         os.environ[env] = "1"
         try:
