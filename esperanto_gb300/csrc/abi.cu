@@ -188,7 +188,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         CK(h, esp::launch_binning(d_pairs, n_pairs, mode == ESP_MODE_HINT ? 1 : 0, h->d_hist,
                                   h->d_order, h->num_sms, st, h->d_ctr + 29,
                                   per_class ? h->d_ctr + 24 : nullptr, paired));
-        h->launches += 6 + (per_class ? 1 : 0) + (paired ? 1 : 0);
+        h->launches += 5 + (per_class ? 1 : 0);  // kernels; the memsets are not counted
         order = h->d_order;
         if (paired) list_len = h->d_ctr + 29;
     }

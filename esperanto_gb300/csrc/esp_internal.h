@@ -139,7 +139,7 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
 
 // Counting-sort the pairs by geometry (descending cost) into `order`; the
 // list length goes to *total (device).  `hist` needs bin_scratch_bytes() of
-// device memory.  6 launches (+1 with bounds, +1 memset with pad).
+// device memory.  5 kernel launches (+1 with bounds) after 1-2 memsets.
 // bounds (optional, 5 device words): the four length classes of the list.
 // pad: every bin padded to an even slot count with NO_PAIR entries (order
 // needs n + bin_pad_slots(n) words), for the two-pairs-per-thread kernel.
