@@ -108,7 +108,7 @@ def test_config1_subset():
 
 
 def test_host_batch_pipeline_chunks():
-    """Host batches of 2^18 pairs and more run as four chunks whose copies
+    """Host batches of 2^18 pairs and more run as eight chunks whose copies
     overlap the neighbouring chunks' kernels: the results equal those of
     unchunked calls on the same pairs, also when the pairs reference the
     arena out of order (each chunk then needs most of the arena), and the
