@@ -572,7 +572,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=16384)
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the per-length-class kernel autotuning (profiling runs)")
