@@ -1,5 +1,5 @@
 // probe.cu -- measured integer issue peaks of this GPU, the denominators of
-// the DP kernels' roofline (the measured peaks cover HBM and bf16
+// the DP kernels' roofline (the measured peaks on file cover HBM and bf16
 // only).  Each probe thread runs 8 independent dependency chains of one
 // instruction kind, long enough that issue, not latency, is the limit; the
 // result is lane-operations per second (a 16x2 operation counts once per

@@ -105,7 +105,7 @@ def test_hint_policy_sweep():
     compare(cases, dirs, mode=B.MODE_HINT)
 
 
-def test_config0_subset_band_and_hint():
+def test_banded_150x214_subset_band_and_hint():
     arena, pairs = B.synth_gotoh(1, 2048, 0)
     cases = []
     for k in range(len(pairs)):
@@ -115,7 +115,7 @@ def test_config0_subset_band_and_hint():
     compare(cases, [0] * len(cases), mode=B.MODE_HINT)
 
 
-def test_config2_subset():
+def test_mixed_length_subset():
     arena, pairs = B.synth_gotoh(3, 1024, 2)
     cases = []
     for k in range(len(pairs)):

@@ -100,7 +100,7 @@ def test_batch_mixed_lengths_with_n(mode):
         assert (int(got[k]["dist"]), int(got[k]["pos"])) == (d, p), k
 
 
-def test_config1_subset():
+def test_myers_150x200_subset():
     arena, pairs = B.synth_myers(2, 20000)
     got = B.myers_batch_host(pairs, arena)
     want = _oracle_batch(arena, pairs, None, B.MYERS_BEST_END)

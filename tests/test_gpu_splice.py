@@ -96,7 +96,7 @@ def _oracle_channel_a(garena, contigs, rarena, reads, cands, r):
                        [int(c["support"]) for c in cs])
 
 
-def test_config3_subset_channel_a():
+def test_split_read_subset_channel_a():
     garena, contigs, rarena, reads, cands = S.synth_splice(4, 600)
     g = S.Genome(garena, contigs)
     out, cig, cells = S.channel_a_batch(g, reads, rarena, cands)
