@@ -318,6 +318,7 @@ __device__ __forceinline__ bool neutral_col(uint32_t q, uint32_t r) {
 // I or D opening a gap run (walk order), I or D extending it.
 enum : int { K_MM = 0, K_MX = 1, K_MZ = 2, K_IO = 3, K_IE = 4, K_DO = 5, K_DE = 6 };
 constexpr int REC_WORDS = 64;  // 512 recorded steps; longer walks re-walk
+constexpr int RUNS_LOCAL = 16;  // CIGAR runs kept in the thread's own list
 
 __device__ __forceinline__ int kind_op(int k) { return k < 3 ? ESP_OP_M : (k < 5 ? ESP_OP_I : ESP_OP_D); }
 
@@ -473,7 +474,22 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
     uint32_t read_start, ref_start, read_end, ref_end;
     int score = 0;
     CigarOut co{cig, cap, false};
-    uint32_t K_runs = 0;  // kept runs, written from index 2 in walk order
+    uint32_t K_runs = 0;  // kept runs in walk order: rr, or from cig[2] when many
+    uint32_t rr[RUNS_LOCAL];
+    // A run goes to the thread's local list; a long CIGAR moves the list to
+    // its slots cig[2..] (CigarOut's capacity rule either way), so short
+    // CIGARs are written once, in final order, with no global read-back.
+    auto emit = [&](uint32_t v) {
+        if (K_runs < RUNS_LOCAL) {
+            rr[K_runs] = v;
+            if (2 + K_runs >= cap) co.overflow = true;
+        } else {
+            if (K_runs == RUNS_LOCAL)
+                for (int k = 0; k < RUNS_LOCAL; k++) co.put(2 + k, rr[k]);
+            co.put(2 + K_runs, v);
+        }
+        K_runs++;
+    };
     int first_op = -1, last_op = -1;  // forward order first / last kept op
     if (N == 0) {
         read_start = (uint32_t)max(F.best_i, 0);
@@ -533,7 +549,7 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
                 if (op == cur_op) {
                     cur_len++;
                 } else {
-                    if (cur_op >= 0) co.put(2 + K_runs++, (cur_len << 4) | (uint32_t)cur_op);
+                    if (cur_op >= 0) emit((cur_len << 4) | (uint32_t)cur_op);
                     cur_op = op;
                     cur_len = 1;
                 }
@@ -551,19 +567,19 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
             read_start = (uint32_t)ts_ia;
             ref_start = (uint32_t)ts_ja;
             score = ts_d;
-            co.put(2, (1u << 4) | (uint32_t)ts_op);
-            K_runs = 1;
+            K_runs = 0;
+            emit((1u << 4) | (uint32_t)ts_op);
             first_op = last_op = ts_op;
         } else {
-            if (cur_op >= 0) co.put(2 + K_runs++, (cur_len << 4) | (uint32_t)cur_op);
+            if (cur_op >= 0) emit((cur_len << 4) | (uint32_t)cur_op);
             if (!found) {  // lead = 0: kept through the last step
                 read_start = (uint32_t)i;
                 ref_start = (uint32_t)j;
             }
         }
     }
-    // reverse the kept runs into forward order
-    if (!co.overflow) {
+    // reverse the kept runs into forward order (a long CIGAR's, in place)
+    if (!co.overflow && K_runs > RUNS_LOCAL) {
         for (uint32_t a = 0, b = K_runs ? K_runs - 1 : 0; a < b; a++, b--) {
             uint32_t t = cig[2 + a];
             cig[2 + a] = cig[2 + b];
@@ -613,7 +629,7 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
         if (read_start > 0) push(ESP_OP_S, read_start);
         if (nl > 0) push(ESP_OP_M, nl);
         for (uint32_t k = 0; k < K_runs; k++) {
-            uint32_t v = cig[2 + k];
+            uint32_t v = K_runs <= RUNS_LOCAL ? rr[K_runs - 1 - k] : cig[2 + k];
             push(v & 15u, v >> 4);
         }
         if (nr > 0) push(ESP_OP_M, nr);

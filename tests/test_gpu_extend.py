@@ -368,3 +368,43 @@ def test_large_batches_run_paired_kernel_with_same_results():
         got = (int(o["score"]), int(o["read_start"]), int(o["read_end"]), int(o["ref_start"]),
                tuple(B.cigar_of(big[1][k], int(o["n_ops"]))))
         assert got == want.key() and bool(o["escalated"]) == esc, k
+
+
+def test_long_cigars_beyond_the_local_run_list():
+    """CIGARs of more than 16 runs (many separated indels) leave the
+    thread's local run list for their output slots; also at a capacity that
+    cuts them off (ESP_ECAP, as before)."""
+    rng = np.random.default_rng(41)
+    cases = []
+    for k in range(64):
+        win = "".join(rng.choice(list("ACGT"), 400))
+        read = list(win[20:380])
+        for p in sorted(rng.choice(np.arange(10, 350, 12), 14 + k % 10, replace=False),
+                        reverse=True):
+            if rng.random() < 0.5:
+                read.pop(int(p))
+            else:
+                read.insert(int(p), str(rng.choice(list("ACGT"))))
+        cases.append(("".join(read).encode(), win.encode(), None))
+    dirs = [k % 3 for k in range(len(cases))]
+    assert compare(cases, dirs, kernels=("thread", "warp", "paired")) == len(cases)
+    want = [O.run_dispatch(r, w, O.Params(edit_dir=d), band=None)[0].key()
+            for (r, w, _), d in zip(cases, dirs)]
+    assert max(len(key[4]) for key in want) > 16
+    # a capacity of 20 ops: longer CIGARs report ESP_ECAP, short ones are exact
+    arena, pairs, n_iv = B.pack_ascii_pairs([c[0] for c in cases], [c[1] for c in cases],
+                                            [0] * len(cases), [-1] * len(cases))
+    for d in range(3):
+        idx = [k for k in range(len(cases)) if dirs[k] == d]
+        out, cig = B.extend_batch_host(pairs[idx], arena, n_iv, E.ExtendParams(edit_dir=d),
+                                       B.MODE_BAND, 20)
+        for row, k in enumerate(idx):
+            n_ops = len(want[k][4])
+            if n_ops > 20:
+                assert int(out[row]["status"]) == -3, k  # ESP_ECAP
+            elif n_ops <= 18:
+                o = out[row]
+                assert int(o["status"]) == 0, k
+                got = (int(o["score"]), int(o["read_start"]), int(o["read_end"]),
+                       int(o["ref_start"]), tuple(B.cigar_of(cig[row], int(o["n_ops"]))))
+                assert got == want[k], k
