@@ -78,7 +78,8 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
                   cudaStream_t st, const uint8_t *d_win_arena, uint64_t win_arena_bytes) {
     h->launches = 0;
     if (n_pairs == 0) return ESP_OK;
-    if (n_pairs > 0xffffffffull - 64) return fail(h, ESP_EINVAL, "batch too large");
+    // list positions are u32, with up to 2^20 padding slots
+    if (n_pairs > 0xffffffffull - (1ull << 21)) return fail(h, ESP_EINVAL, "batch too large");
     int rc;
     if (h->warp_max < 0) {
         const char *v = getenv("ESP_WARP_MAX");
