@@ -1101,8 +1101,11 @@ __device__ __forceinline__ void dp_cols2(Strip2 &S, const uint32_t oe1, const ui
             } else {
                 rbr[(ptrdiff_t)(plo - lo7) * 32] = packed;
             }
-            *tbA = __byte_perm(wa, wb, 0x5410);
-            *tbB = __byte_perm(wa, wb, 0x7632);
+            // streaming stores: the traceback words make way in L2 for the
+            // row buffer (measured +1.8 % here; the one-pair kernel's own
+            // stores measured 0.8 % slower so)
+            __stcs(tbA, __byte_perm(wa, wb, 0x5410));
+            __stcs(tbB, __byte_perm(wa, wb, 0x7632));
             tbA += 32;
             tbB += 32;
             rbr += 32;
