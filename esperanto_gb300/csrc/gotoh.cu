@@ -476,13 +476,13 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
     CigarOut co{cig, cap, false};
     uint32_t K_runs = 0;  // kept runs in walk order: rr, or from cig[2] when many
     uint32_t rr[RUNS_LOCAL];
-    // A run goes to the thread's local list; a long CIGAR moves the list to
-    // its slots cig[2..] (CigarOut's capacity rule either way), so short
-    // CIGARs are written once, in final order, with no global read-back.
+    // A run goes to the thread's local list, so short CIGARs are written
+    // once, in final order, with no global read-back, and need only their
+    // final length in capacity; a long CIGAR moves the list to its slots
+    // cig[2..] (and needs them: it is reversed there in place).
     auto emit = [&](uint32_t v) {
         if (K_runs < RUNS_LOCAL) {
             rr[K_runs] = v;
-            if (2 + K_runs >= cap) co.overflow = true;
         } else {
             if (K_runs == RUNS_LOCAL)
                 for (int k = 0; k < RUNS_LOCAL; k++) co.put(2 + k, rr[k]);

@@ -408,3 +408,36 @@ def test_long_cigars_beyond_the_local_run_list():
                 got = (int(o["score"]), int(o["read_start"]), int(o["read_end"]),
                        int(o["ref_start"]), tuple(B.cigar_of(cig[row], int(o["n_ops"]))))
                 assert got == want[k], k
+
+
+def test_cigar_capacity_exact_fit():
+    """A CIGAR of up to 16 runs needs exactly its final length in capacity:
+    a stride equal to the oracle's op count succeeds bit-exactly, one less
+    reports ESP_ECAP."""
+    rng = np.random.default_rng(43)
+    for k in range(24):
+        win = "".join(rng.choice(list("ACGT"), 260))
+        read = list(win[30:230])
+        for p in sorted(rng.choice(np.arange(20, 180, 15), 1 + k % 6, replace=False),
+                        reverse=True):
+            if rng.random() < 0.5:
+                read.pop(int(p))
+            else:
+                read.insert(int(p), str(rng.choice(list("ACGT"))))
+        read = ("".join(rng.choice(list("ACGT"), 1 + k % 4)) + "".join(read)).encode()
+        want = O.run_dispatch(read, win.encode(), O.Params(), band=None)[0].key()
+        n_ops = len(want[4])
+        arena, pairs, n_iv = B.pack_ascii_pairs([read], [win.encode()], [0], [-1])
+        for kern in ("warp", "thread"):
+            buf = kernel_buffer(kern)
+            out, cig = B.extend_batch_host(pairs, arena, n_iv, E.ExtendParams(), B.MODE_BAND,
+                                           n_ops, buf=buf)
+            o = out[0]
+            assert int(o["status"]) == 0, (k, n_ops, kern)
+            got = (int(o["score"]), int(o["read_start"]), int(o["read_end"]),
+                   int(o["ref_start"]), tuple(B.cigar_of(cig[0], int(o["n_ops"]))))
+            assert got == want, (k, kern)
+            if n_ops > 1:
+                out, _ = B.extend_batch_host(pairs, arena, n_iv, E.ExtendParams(), B.MODE_BAND,
+                                             n_ops - 1, buf=buf)
+                assert int(out[0]["status"]) == -3, (k, kern)  # ESP_ECAP
