@@ -30,14 +30,16 @@ EDIT_OFF, EDIT_AG, EDIT_TC = 0, 1, 2
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with gcc into oracle/_build (portable C, -O2)."""
+    """Compile the oracle with gcc into oracle/_build (portable C, -O3, the
+    optimisation level of the reference's own release builds)."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    srcs = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, "esp_oracle.h")]
+    srcs = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, "esp_oracle.h"),
+                                                        os.path.abspath(__file__)]  # flags
     if not force and os.path.exists(LIB_PATH):
         lib_m = os.path.getmtime(LIB_PATH)
         if all(os.path.getmtime(s) <= lib_m for s in srcs):
             return LIB_PATH
-    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
+    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
            "-o", LIB_PATH + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES] + ["-lm"]
     subprocess.run(cmd, check=True)
     os.replace(LIB_PATH + ".tmp", LIB_PATH)
