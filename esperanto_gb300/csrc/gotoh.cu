@@ -1217,8 +1217,8 @@ __device__ __noinline__ void fill2_call(const GotohConst &K, const uint32_t *__r
                                         const PairSetup &A, const PairSetup &B, uint32_t *tbA,
                                         uint32_t *tbB, uint32_t *rb, FillResult &FA,
                                         FillResult &FB) {
-    dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win.arena, A.win.pos, B.win.pos, tbA, tbB, A.sw,
-             reinterpret_cast<uint2 *>(rb), FA, FB);
+    dp_fill2(K, s_lut, A.m, A.n, A.g, A.read, B.read, A.win.arena, A.win.pos, B.win.pos, tbA,
+             tbB, A.sw, reinterpret_cast<uint2 *>(rb), FA, FB);
 }
 
 __device__ __noinline__ void finish_call(const GotohJob &job, const GotohConst &K,
