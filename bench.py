@@ -34,6 +34,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+import workloads as W  # noqa: E402  (seeded inputs; no library is loaded at import)
+
 # Integer ops per cell of the DP recurrence in its scalar 32-bit form (E 3,
 # F 3, tag clears 2, LUT select + diag add + floor 3, H key 3, H tag 1,
 # traceback-bit selects 2, row max 1; the multiply-adds that accumulate the
@@ -59,23 +61,21 @@ DEFAULT_PAIRS = {0: 65536, 1: 1048576, 2: 4194304, 3: 524288}
 SEEDS = {0: 1, 1: 2, 2: 3, 3: 4}
 
 
-def int_peak(L, buf, lanes=1):
+def int_peak(device, lanes=1):
     """Measured integer-ALU issue peak of this GPU (lane-ops/s): the slower
-    of the 3-input-logic and integer-max probe streams (esp_int_peaks); for
-    the 16x2 SIMD kernel (lanes = 2) the slowest of those and the 16x2
-    add-max / 3-way-max streams (esp_simd16_peaks), times two 16-bit cells
-    per lane-op."""
-    v = [C.c_double() for _ in range(4)]
-    buf.check(L.esp_int_peaks(buf.handle, *[C.byref(x) for x in v]))
-    lop3, imnmx, iadd, imad = (x.value for x in v)
+    of the 3-input-logic and integer-max probe streams (esp_probe_int_peaks);
+    for the 16x2 SIMD kernel (lanes = 2) the slowest of those and the 16x2
+    add-max / 3-way-max streams (esp_probe_simd16_peaks), times two 16-bit
+    cells per lane-op."""
+    import workloads as W
+    lop3, imnmx, iadd, imad = W.int_peaks(device)
     probe = {"lop3": lop3 / 1e12, "imnmx": imnmx / 1e12, "iadd": iadd / 1e12,
              "imad": imad / 1e12}
     peak = min(lop3, imnmx)
     if lanes == 2:
-        s = [C.c_double() for _ in range(2)]
-        buf.check(L.esp_simd16_peaks(buf.handle, *[C.byref(x) for x in s]))
-        probe["addmax_s16x2"], probe["max3_s16x2"] = s[0].value / 1e12, s[1].value / 1e12
-        peak = 2 * min(peak, s[0].value, s[1].value)
+        addmax, max3 = W.simd16_peaks(device)
+        probe["addmax_s16x2"], probe["max3_s16x2"] = addmax / 1e12, max3 / 1e12
+        peak = 2 * min(peak, addmax, max3)
     return peak, probe
 
 
@@ -172,7 +172,7 @@ class GotohWorkload(Workload):
         from esperanto_gb300.extend import ExtendParams
         L = N.lib()
         self.stride = 32
-        arena, pairs = B.synth_gotoh(seed, n, self.config)
+        arena, pairs = W.synth_gotoh(seed, n, self.config)
         self.cells = B.cells_of(pairs)
         self.n = n
         d_arena = torch.from_numpy(arena).to(dev)
@@ -241,7 +241,7 @@ class GotohWorkload(Workload):
         from esperanto_gb300 import batch as B
         from esperanto_gb300.extend import ExtendParams
         L = N.lib()
-        arena, pairs = B.synth_gotoh(seed, sample, self.config)
+        arena, pairs = W.synth_gotoh(seed, sample, self.config)
         cases = []
         for k in range(sample):
             r = B._ASCII[B.unpack_codes(arena, int(pairs["read_pos"][k]),
@@ -304,7 +304,7 @@ class GotohWorkload(Workload):
         import oracle as O
         from esperanto_gb300 import batch as B
         O.build()
-        arena, pairs = B.synth_gotoh(seed, sample, self.config)
+        arena, pairs = W.synth_gotoh(seed, sample, self.config, lib=O.synth_lib())
         end = int((pairs["win_pos"] + pairs["win_len"]).max())
         seq = B._ASCII[B.unpack_codes(arena, 0, end)]
 
@@ -331,7 +331,7 @@ class MyersWorkload(Workload):
         from esperanto_gb300 import _native as N
         from esperanto_gb300 import batch as B
         L = N.lib()
-        arena, pairs = B.synth_myers(seed, n)
+        arena, pairs = W.synth_myers(seed, n)
         self.n = n
         self.cells = int((pairs["read_len"].astype(np.int64) * pairs["text_len"]).sum())
         d_arena = torch.from_numpy(arena).to(dev)
@@ -365,7 +365,7 @@ class MyersWorkload(Workload):
         from esperanto_gb300 import batch as B
         O.build()
         sample *= 16
-        arena, pairs = B.synth_myers(seed, sample)
+        arena, pairs = W.synth_myers(seed, sample, lib=O.synth_lib())
         end = int((pairs["text_pos"] + pairs["text_len"]).max())
         seq = B._ASCII[B.unpack_codes(arena, 0, end)]
 
@@ -391,7 +391,7 @@ class SpliceWorkload(Workload):
         from esperanto_gb300 import split as S
         from esperanto_gb300.extend import ExtendParams
         L = N.lib()
-        garena, contigs, rarena, reads, cands = S.synth_splice(seed, n)
+        garena, contigs, rarena, reads, cands = W.synth_splice(seed, n)
         self.n = n
         self.genome = S.Genome(garena, contigs, buf=buf)
         sp, p = S.SpliceParams()._c(), ExtendParams()._c()
@@ -447,7 +447,7 @@ class SpliceWorkload(Workload):
         from esperanto_gb300 import split as S
         O.build()
         sample = max(64, sample // 16)
-        garena, contigs, rarena, reads, cands = S.synth_splice(seed, sample)
+        garena, contigs, rarena, reads, cands = W.synth_splice(seed, sample, lib=O.synth_lib())
         ra = B._ASCII[B.unpack_codes(rarena, 0, len(reads) * 150)]
 
         def run():
@@ -469,12 +469,12 @@ def serve_bench(args):
     torch.cuda.set_device(0)
     buf = ExtendBuffer(0)
     t0 = time.perf_counter()
-    garena, contigs = SV.synth_genome(5, args.genome_bases, 24)
+    garena, contigs = W.synth_genome(5, args.genome_bases, 24)
     genome = Genome(garena, contigs, buf=buf)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(5)
     sizes = np.exp(rng.uniform(np.log(1000), np.log(65536), args.pool)).astype(int)
-    pool = [SV.synth_request(5, k, garena, contigs, int(n)) for k, n in enumerate(sizes)]
+    pool = [W.synth_request(5, k, garena, contigs, int(n)) for k, n in enumerate(sizes)]
     srv = SV.Server(genome, n_streams=args.streams, max_reads=65536, mem_budget=16 << 30)
     # warm up every slot
     for t in [srv.submit(*pool[k % len(pool)]) for k in range(2 * args.streams)]:
@@ -660,7 +660,7 @@ def main():
 
     peaks, src = load_peaks()
     lanes = getattr(wl, "lanes", 1)
-    peak_ops, probe = int_peak(L, buf, lanes)
+    peak_ops, probe = int_peak(local, lanes)
     achieved_ops = wl.cells * wl.ops_per_cell / (ms / 1e3)
     traffic = None
     if config in TRAFFIC_BYTES and n_pairs == DEFAULT_PAIRS[config]:
@@ -700,10 +700,10 @@ def main():
                      "peak": peak_ops / 1e12, "unit": "Tops/s",
                      "frac": achieved_ops / peak_ops, "traffic": traffic,
                      "traffic_source": TRAFFIC_SOURCE.get(config),
-                     "peak_source": "measured on this GPU (esp_int_peaks: independent streams "
+                     "peak_source": "measured on this GPU (esp_probe_int_peaks: independent streams "
                                     "of 3-input logic / integer max, the ALU-pipe issue rate)"
                                     + ("; with the 16x2 add-max / 3-way-max streams "
-                                       "(esp_simd16_peaks) for the two-pairs-per-thread "
+                                       "(esp_probe_simd16_peaks) for the two-pairs-per-thread "
                                        "kernel, x 2 cells per lane-op" if lanes == 2 else ""),
                      "simd_lanes": lanes,
                      "probe_tops": probe, "ops_per_cell": wl.ops_per_cell,

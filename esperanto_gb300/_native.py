@@ -160,8 +160,6 @@ def lib():
                                          vp, C.c_uint64, vp, vp]
     L.esp_batch_myers_host.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
                                        C.c_uint64, vp]
-    L.esp_synth_myers_size.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]
-    L.esp_synth_myers.argtypes = [C.c_uint64, C.c_uint64, vp, C.c_uint64, vp]
     L.esp_genome_create.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint32, vp, C.c_uint64,
                                     C.POINTER(vp)]
     L.esp_genome_destroy.argtypes = [vp]
@@ -180,8 +178,6 @@ def lib():
     L.esp_batch_autotune.argtypes = [vp, C.c_int, vp, C.c_uint64, vp, C.c_uint64, vp,
                                      C.c_uint64, C.POINTER(BatchLimitsC),
                                      C.POINTER(ExtendParamsC), vp, vp, C.c_uint32, vp, vp, vp]
-    L.esp_int_peaks.argtypes = [vp] + [C.POINTER(C.c_double)] * 4
-    L.esp_simd16_peaks.argtypes = [vp] + [C.POINTER(C.c_double)] * 2
     L.esp_paidx_scan.argtypes = [vp, C.c_uint64, C.POINTER(PaidxInfoC), C.c_char_p, sz]
     L.esp_paidx_contigs.argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint32, vp,
                                     C.c_uint64, vp, C.c_uint64]
@@ -204,14 +200,8 @@ def lib():
                                   C.POINTER(C.c_double)]
     L.esp_server_close.argtypes = [vp]
     L.esp_server_destroy.argtypes = [vp]
-    L.esp_synth_genome.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, vp, C.c_uint64, vp]
-    L.esp_synth_serve_reads.argtypes = [C.c_uint64, C.c_uint64, vp, vp, C.c_uint32, C.c_uint64,
-                                        vp, C.c_uint64, vp]
     L.esp_last_cells.argtypes = [vp]
     L.esp_last_cells.restype = C.c_uint64
-    L.esp_synth_splice_size.argtypes = [C.c_uint64, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3
-    L.esp_synth_splice.argtypes = [C.c_uint64, C.c_uint64, vp, C.c_uint64, vp, vp, C.c_uint64,
-                                   vp, vp, C.c_uint64]
     _lib = L
     return L
 

@@ -111,25 +111,6 @@ def decode_pair(arena: np.ndarray, pair, n_iv: Optional[np.ndarray] = None) -> T
     return r.tobytes(), w.tobytes()
 
 
-def synth_gotoh(seed: int, n_pairs: int, config: int):
-    """Seeded Gotoh workload, shape 0 (150 x 214 banded) or 2 (mixed length):
-    (arena, pairs)."""
-    L = N.lib()
-    L.esp_synth_gotoh_size.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64)]
-    L.esp_synth_gotoh.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p, C.c_uint64,
-                                  C.c_void_p]
-    nb = C.c_uint64()
-    rc = L.esp_synth_gotoh_size(seed, n_pairs, config, C.byref(nb))
-    if rc:
-        raise N.EspError(rc, "esp_synth_gotoh_size")
-    arena = np.zeros(nb.value, np.uint8)
-    pairs = np.zeros(n_pairs, PAIR_DTYPE)
-    rc = L.esp_synth_gotoh(seed, n_pairs, config, arena.ctypes.data, nb.value, pairs.ctypes.data)
-    if rc:
-        raise N.EspError(rc, "esp_synth_gotoh")
-    return arena, pairs
-
-
 def cells_of(pairs: np.ndarray, mode: int = MODE_BAND, escalated: Optional[np.ndarray] = None) -> int:
     """DP cells (sum over rows of the in-window width, extend.rs:653-696)."""
     m = pairs["read_len"].astype(np.int64)
@@ -188,21 +169,6 @@ def extend_batch_host(pairs: np.ndarray, arena: np.ndarray, n_iv: Optional[np.nd
 
 def cigar_of(cig_row: np.ndarray, n_ops: int):
     return [("MIDNS"[int(o) & 15], int(o) >> 4) for o in cig_row[:n_ops]]
-
-
-def synth_myers(seed: int, n_pairs: int):
-    """Seeded Myers workload (150-bp queries vs 200-bp texts): (arena, myers pairs)."""
-    L = N.lib()
-    nb = C.c_uint64()
-    rc = L.esp_synth_myers_size(seed, n_pairs, C.byref(nb))
-    if rc:
-        raise N.EspError(rc, "esp_synth_myers_size")
-    arena = np.zeros(nb.value, np.uint8)
-    pairs = np.zeros(n_pairs, MYERS_PAIR_DTYPE)
-    rc = L.esp_synth_myers(seed, n_pairs, arena.ctypes.data, nb.value, pairs.ctypes.data)
-    if rc:
-        raise N.EspError(rc, "esp_synth_myers")
-    return arena, pairs
 
 
 def pack_ascii_myers(reads, texts):

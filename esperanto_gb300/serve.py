@@ -94,31 +94,6 @@ class Server:
             pass
 
 
-def synth_genome(seed: int, total_bases: int, n_contigs: int):
-    """Uniform-ACGT genome: (arena, contigs)."""
-    stride = ((total_bases + n_contigs - 1) // n_contigs + 3) // 4 * 4
-    arena = np.zeros(stride * n_contigs // 4 + 16, np.uint8)
-    contigs = np.zeros(n_contigs, CONTIG_DTYPE)
-    rc = N.lib().esp_synth_genome(seed, total_bases, n_contigs, arena.ctypes.data, len(arena),
-                                  contigs.ctypes.data)
-    if rc:
-        raise N.EspError(rc, "esp_synth_genome")
-    return arena, contigs
-
-
-def synth_request(seed: int, request: int, genome_arena: np.ndarray, contigs: np.ndarray,
-                  n_reads: int):
-    """Paired-end request reads: (read arena, serve reads)."""
-    arena = np.zeros((n_reads * 150 + 3) // 4 + 16, np.uint8)
-    reads = np.zeros(n_reads, SERVE_READ_DTYPE)
-    rc = N.lib().esp_synth_serve_reads(seed, request, genome_arena.ctypes.data,
-                                       contigs.ctypes.data, len(contigs), n_reads,
-                                       arena.ctypes.data, len(arena), reads.ctypes.data)
-    if rc:
-        raise N.EspError(rc, "esp_synth_serve_reads")
-    return arena, reads
-
-
 def serve_pairs(reads: np.ndarray, contigs: np.ndarray) -> np.ndarray:
     """The esp_pair records the server builds for a request (for checks)."""
     pairs = np.zeros(len(reads), B.PAIR_DTYPE)

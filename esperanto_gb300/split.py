@@ -325,24 +325,3 @@ def channel_a_batch(genome: Genome, reads: np.ndarray, read_arena: np.ndarray,
     buf.check(rc)
     cells = int(N.lib().esp_last_cells(buf.handle))
     return out, cig[:len(reads) * cigar_stride].reshape(len(reads), cigar_stride), cells
-
-
-def synth_splice(seed: int, n_reads: int):
-    """Seeded splice workload (524,288-read rescue batch shape):
-    (genome_arena, contigs, read_arena, reads, cands)."""
-    L = N.lib()
-    gb, rb, nc = C.c_uint64(), C.c_uint64(), C.c_uint64()
-    rc = L.esp_synth_splice_size(seed, n_reads, C.byref(gb), C.byref(rb), C.byref(nc))
-    if rc:
-        raise N.EspError(rc, "esp_synth_splice_size")
-    garena = np.zeros(gb.value, np.uint8)
-    contigs = np.zeros(n_reads, CONTIG_DTYPE)
-    rarena = np.zeros(rb.value, np.uint8)
-    reads = np.zeros(n_reads, SPLICE_READ_DTYPE)
-    cands = np.zeros(nc.value, SPLICE_CAND_DTYPE)
-    rc = L.esp_synth_splice(seed, n_reads, garena.ctypes.data, gb.value, contigs.ctypes.data,
-                            rarena.ctypes.data, rb.value, reads.ctypes.data, cands.ctypes.data,
-                            nc.value)
-    if rc:
-        raise N.EspError(rc, "esp_synth_splice")
-    return garena, contigs, rarena, reads, cands

@@ -29,19 +29,37 @@ OP_CHARS = "MIDNS"
 EDIT_OFF, EDIT_AG, EDIT_TC = 0, 1, 2
 
 
+SYNTH_SRC = os.path.join(os.path.dirname(HERE), "workloads", "synth.cpp")
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc into oracle/_build (portable C, -O3, the
-    optimisation level of the reference's own release builds)."""
+    optimisation level of the reference's own release builds).  The library
+    also carries a g++ build of the seeded workload generators
+    (workloads/synth.cpp), so that the benchmark's reference arm makes its
+    inputs without loading any library of the GPU path."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    srcs = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, "esp_oracle.h"),
-                                                        os.path.abspath(__file__)]  # flags
+    inc = [os.path.join(os.path.dirname(HERE), "workloads"),
+           os.path.join(os.path.dirname(HERE), "include")]
+    deps = ([os.path.join(HERE, s) for s in SOURCES] + [SYNTH_SRC, os.path.join(HERE, "esp_oracle.h"),
+            os.path.abspath(__file__)] + [os.path.join(d, h) for d, h in
+                                          ((inc[0], "esp_workloads.h"), (inc[1], "esperanto_gb300.h"))])
     if not force and os.path.exists(LIB_PATH):
         lib_m = os.path.getmtime(LIB_PATH)
-        if all(os.path.getmtime(s) <= lib_m for s in srcs):
+        if all(os.path.getmtime(s) <= lib_m for s in deps):
             return LIB_PATH
-    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
-           "-o", LIB_PATH + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES] + ["-lm"]
-    subprocess.run(cmd, check=True)
+    objs = []
+    for src in SOURCES:
+        obj = os.path.join(BUILD_DIR, src + ".o")
+        subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-pthread", "-Wall", "-c",
+                        os.path.join(HERE, src), "-o", obj], check=True)
+        objs.append(obj)
+    obj = os.path.join(BUILD_DIR, "synth.cpp.o")
+    subprocess.run(["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-I", inc[0], "-I", inc[1],
+                    "-c", SYNTH_SRC, "-o", obj], check=True)
+    objs.append(obj)
+    subprocess.run(["g++", "-shared", "-pthread", "-o", LIB_PATH + ".tmp"] + objs + ["-lm"],
+                   check=True)
     os.replace(LIB_PATH + ".tmp", LIB_PATH)
     return LIB_PATH
 
@@ -151,6 +169,13 @@ def lib():
         L.free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
+
+
+def synth_lib():
+    """This library's build of the workload generators, bound like
+    workloads.synth_lib() (pass it as ``lib=`` to the workloads generators)."""
+    import workloads
+    return workloads.bind_synth(lib())
 
 
 def _libc_free(ptr):

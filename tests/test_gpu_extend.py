@@ -16,6 +16,7 @@ if not torch.cuda.is_available():
 import esperanto_gb300 as E  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
 from gpu_helpers import _compare, compare, kernel_buffer  # noqa: E402
+import workloads as W  # noqa: E402
 
 
 def _gpu_kind(kind, case):
@@ -106,7 +107,7 @@ def test_hint_policy_sweep():
 
 
 def test_banded_150x214_subset_band_and_hint():
-    arena, pairs = B.synth_gotoh(1, 2048, 0)
+    arena, pairs = W.synth_gotoh(1, 2048, 0)
     cases = []
     for k in range(len(pairs)):
         r, w = B.decode_pair(arena, pairs[k])
@@ -116,7 +117,7 @@ def test_banded_150x214_subset_band_and_hint():
 
 
 def test_mixed_length_subset():
-    arena, pairs = B.synth_gotoh(3, 1024, 2)
+    arena, pairs = W.synth_gotoh(3, 1024, 2)
     cases = []
     for k in range(len(pairs)):
         r, w = B.decode_pair(arena, pairs[k])
@@ -126,7 +127,7 @@ def test_mixed_length_subset():
 
 def test_batch_direct_synth_matches_oracle_batch():
     # the synthetic arena straight into the batch API (no ASCII round trip)
-    arena, pairs = B.synth_gotoh(11, 4096, 0)
+    arena, pairs = W.synth_gotoh(11, 4096, 0)
     out, cig = B.extend_batch_host(pairs, arena, params=E.ExtendParams(), mode=B.MODE_BAND,
                                    cigar_stride=32)
     assert (out["status"] == 0).all()
@@ -187,7 +188,7 @@ def test_graph_replay_of_identical_device_batches():
     from esperanto_gb300 import _native as N
     from esperanto_gb300.extend import ExtendBuffer, ExtendParams
     n = 20000  # above the warp-per-pair size: binning + persistent kernel
-    sets = [B.synth_gotoh(s, n, 2) for s in (11, 12)]
+    sets = [W.synth_gotoh(s, n, 2) for s in (11, 12)]
     size = max(a.nbytes for a, _ in sets)
     lim = N.BatchLimitsC(300, 300 + 256, 128)
     p = ExtendParams()._c()
@@ -272,7 +273,7 @@ def test_paired_kernel_variants_on_mixed_batch():
     """Both paired variants (3 and 4 blocks per SM) on the mixed-length
     workload equal the one-pair kernel bit for bit (results and CIGARs)."""
     from esperanto_gb300.extend import ExtendBuffer
-    ar, pr = B.synth_gotoh(31, 50000, 2)
+    ar, pr = W.synth_gotoh(31, 50000, 2)
     want = B.extend_batch_host(pr, ar, cigar_stride=32, buf=kernel_buffer("thread"))
     for v in (2, 3):
         buf = ExtendBuffer()
@@ -293,7 +294,7 @@ def test_autotune_per_length_class():
     from esperanto_gb300 import _native as N
     from esperanto_gb300.extend import ExtendBuffer, ExtendParams
     n = 30000
-    ar, pr = B.synth_gotoh(21, n, 2)
+    ar, pr = W.synth_gotoh(21, n, 2)
     wo, wc = B.extend_batch_host(pr, ar, cigar_stride=32)
     lim = N.BatchLimitsC(300, 300 + 256, 128)
     p = ExtendParams()._c()
@@ -327,7 +328,7 @@ def test_hint_escalation_decisions_match_oracle():
     rate is then the oracle's too."""
     from gpu_helpers import gpu_batch
     for shape, n in ((0, 1024), (2, 512)):
-        arena, pairs = B.synth_gotoh(7, n, shape)
+        arena, pairs = W.synth_gotoh(7, n, shape)
         cases = []
         for k in range(n):
             r, w = B.decode_pair(arena, pairs[k])
@@ -348,7 +349,7 @@ def test_large_batches_run_paired_kernel_with_same_results():
     from esperanto_gb300.extend import ExtendBuffer
     for mode, env, n in ((B.MODE_BAND, "ESP_GOTOH_VARIANT", 1 << 21),
                          (B.MODE_HINT, "ESP_GOTOH_HINT_VARIANT", 1 << 20)):
-        arena, pairs = B.synth_gotoh(13, n, 0)
+        arena, pairs = W.synth_gotoh(13, n, 0)
         big = B.extend_batch_host(pairs, arena, mode=mode, cigar_stride=32, buf=ExtendBuffer())
         os.environ[env] = "1"
         try:

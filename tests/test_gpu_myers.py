@@ -16,6 +16,7 @@ import oracle as O  # noqa: E402
 from esperanto_gb300 import EspError  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
 from esperanto_gb300 import engine_myers, myers_ea  # noqa: E402
+import workloads as W  # noqa: E402
 
 
 def _case(rng, m, n, alpha="ACGT"):
@@ -101,7 +102,7 @@ def test_batch_mixed_lengths_with_n(mode):
 
 
 def test_myers_150x200_subset():
-    arena, pairs = B.synth_myers(2, 20000)
+    arena, pairs = W.synth_myers(2, 20000)
     got = B.myers_batch_host(pairs, arena)
     want = _oracle_batch(arena, pairs, None, B.MYERS_BEST_END)
     assert [(int(g["dist"]), int(g["pos"])) for g in got] == want
@@ -113,7 +114,7 @@ def test_host_batch_pipeline_chunks():
     unchunked calls on the same pairs, also when the pairs reference the
     arena out of order (each chunk then needs most of the arena), and the
     oracle on a sample."""
-    arena, pairs = B.synth_myers(5, 300000)
+    arena, pairs = W.synth_myers(5, 300000)
     rng = np.random.default_rng(3)
     for order in (np.arange(len(pairs)), rng.permutation(len(pairs))):
         p = pairs[order]

@@ -14,11 +14,12 @@ from esperanto_gb300 import EspError  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
 from esperanto_gb300 import serve as SV  # noqa: E402
 from esperanto_gb300.split import Genome  # noqa: E402
+import workloads as W  # noqa: E402
 
 
 @pytest.fixture(scope="module")
 def setup():
-    garena, contigs = SV.synth_genome(5, 4_000_000, 4)
+    garena, contigs = W.synth_genome(5, 4_000_000, 4)
     g = Genome(garena, contigs)
     srv = SV.Server(g, n_streams=3, max_reads=32768, mem_budget=2 << 30)
     yield garena, contigs, g, srv
@@ -33,7 +34,7 @@ def _key(t, k):
 
 def test_alone_equals_mix_equals_batch_and_oracle(setup):
     garena, contigs, g, srv = setup
-    arena, reads = SV.synth_request(5, 1, garena, contigs, 3000)
+    arena, reads = W.synth_request(5, 1, garena, contigs, 3000)
     alone = srv.submit(arena, reads)
     st, lat = srv.wait(alone)
     assert st == 0 and lat > 0
@@ -41,7 +42,7 @@ def test_alone_equals_mix_equals_batch_and_oracle(setup):
     # the same request in a mix of concurrent requests of other sizes
     mix = []
     for k, n in enumerate([800, 20000, 3000, 12000, 500, 30000, 7000, 1000]):
-        a2, r2 = SV.synth_request(5, 100 + k, garena, contigs, n)
+        a2, r2 = W.synth_request(5, 100 + k, garena, contigs, n)
         mix.append(srv.submit(a2, r2))
         if k == 3:
             again = srv.submit(arena, reads)
@@ -71,18 +72,18 @@ def test_alone_equals_mix_equals_batch_and_oracle(setup):
 
 def test_admission_and_close(setup):
     garena, contigs, g, srv = setup
-    arena, reads = SV.synth_request(5, 7, garena, contigs, 40000)  # > max_reads
+    arena, reads = W.synth_request(5, 7, garena, contigs, 40000)  # > max_reads
     with pytest.raises(EspError):
         srv.submit(arena, reads)
     srv2 = SV.Server(g, n_streams=1, max_reads=32768, mem_budget=1 << 30)
     # requests are built first so that all six are queued within microseconds
     # and the single slot is still busy with the first when close() lands
-    reqs = [SV.synth_request(5, 200 + k, garena, contigs, 30000) for k in range(6)]
+    reqs = [W.synth_request(5, 200 + k, garena, contigs, 30000) for k in range(6)]
     ts = [srv2.submit(*r) for r in reqs]
     srv2.close()
     sts = [srv2.wait(t)[0] for t in ts]
     assert sts[0] == 0                      # already admitted: finishes normally
     assert any(s == -8 for s in sts[1:])    # still queued at close: ESP_ECLOSED
     with pytest.raises(EspError):
-        srv2.submit(*SV.synth_request(5, 300, garena, contigs, 100))
+        srv2.submit(*W.synth_request(5, 300, garena, contigs, 100))
     srv2.destroy()

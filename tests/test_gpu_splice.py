@@ -15,6 +15,7 @@ import oracle as O  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
 from esperanto_gb300 import split as S  # noqa: E402
 from golden_check import load  # noqa: E402
+import workloads as W  # noqa: E402
 
 
 def _oracle_retry(seq, read, ts, start, end, minus, sig, sup):
@@ -97,7 +98,7 @@ def _oracle_channel_a(garena, contigs, rarena, reads, cands, r):
 
 
 def test_split_read_subset_channel_a():
-    garena, contigs, rarena, reads, cands = S.synth_splice(4, 600)
+    garena, contigs, rarena, reads, cands = W.synth_splice(4, 600)
     g = S.Genome(garena, contigs)
     out, cig, cells = S.channel_a_batch(g, reads, rarena, cands)
     assert cells > 0

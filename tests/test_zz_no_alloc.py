@@ -26,6 +26,7 @@ import refgen as R  # noqa: E402
 from esperanto_gb300 import _native as N  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
 from esperanto_gb300.extend import ExtendBuffer, ExtendParams  # noqa: E402
+import workloads as W  # noqa: E402
 
 ESP_ESCRATCH = -9
 
@@ -43,7 +44,7 @@ def _lib():
 def _batch():
     """Seeded pairs: the plain 150 x 214 workload plus shapes with N runs,
     clamped bands and m > n (the reference's own sweep shapes)."""
-    arena0, pairs0 = B.synth_gotoh(5, 1536, 0)
+    arena0, pairs0 = W.synth_gotoh(5, 1536, 0)
     reads, wins, offs, halfs = [], [], [], []
     for k in range(len(pairs0)):
         r, w = B.decode_pair(arena0, pairs0[k])

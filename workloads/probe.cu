@@ -1,6 +1,6 @@
-// probe.cu -- measured integer issue peaks of this GPU, the denominators of
-// the DP kernels' roofline (the measured peaks on file cover HBM and bf16
-// only).  Each probe thread runs 8 independent dependency chains of one
+// probe.cu -- measured integer issue peaks of a GPU, the denominators of the
+// DP kernels' roofline (the measured peaks on file cover HBM and bf16 only).
+// Benchmark tooling: built into its own library, not the alignment path's.  Each probe thread runs 8 independent dependency chains of one
 // instruction kind, long enough that issue, not latency, is the limit; the
 // result is lane-operations per second (a 16x2 operation counts once per
 // 32-bit lane: it updates two 16-bit values).
@@ -8,7 +8,7 @@
 
 #include <cstdint>
 
-#include "esp_host.h"
+#include "esp_workloads.h"
 
 namespace {
 
@@ -68,29 +68,37 @@ int run(int sms, cudaStream_t st, uint32_t *sink, double *out) {
     return ESP_OK;
 }
 
-}  // namespace
+using ProbeFn = int (*)(int, cudaStream_t, uint32_t *, double *);
 
-extern "C" int esp_simd16_peaks(esp_handle *h, double *addmax, double *max3) {
-    if (!h || !addmax || !max3) return ESP_EINVAL;
-    CK(h, cudaSetDevice(h->device));
+// Runs the probes `fns` on `device`, one result each.
+int run_probes(int device, int n, const ProbeFn *fns, double **out) {
+    if (cudaSetDevice(device) != cudaSuccess) return ESP_ECUDA;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return ESP_ECUDA;
+    cudaStream_t st = nullptr;
     uint32_t *sink = nullptr;
-    CK(h, cudaMalloc((void **)&sink, 4));
-    int rc = run<4>(h->num_sms, h->stream, sink, addmax);
-    if (rc == ESP_OK) rc = run<5>(h->num_sms, h->stream, sink, max3);
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return ESP_ECUDA;
+    int rc = cudaMalloc((void **)&sink, 4) == cudaSuccess ? ESP_OK : ESP_ECUDA;
+    for (int k = 0; k < n && rc == ESP_OK; k++) rc = fns[k](sms, st, sink, out[k]);
     cudaFree(sink);
-    return rc == ESP_OK ? ESP_OK : fail(h, rc, "16x2 peak probe failed");
+    cudaStreamDestroy(st);
+    return rc;
 }
 
-extern "C" int esp_int_peaks(esp_handle *h, double *lop3, double *imnmx, double *iadd,
-                             double *imad) {
-    if (!h || !lop3 || !imnmx || !iadd || !imad) return ESP_EINVAL;
-    CK(h, cudaSetDevice(h->device));
-    uint32_t *sink = nullptr;
-    CK(h, cudaMalloc((void **)&sink, 4));
-    int rc = run<0>(h->num_sms, h->stream, sink, lop3);
-    if (rc == ESP_OK) rc = run<1>(h->num_sms, h->stream, sink, imnmx);
-    if (rc == ESP_OK) rc = run<2>(h->num_sms, h->stream, sink, iadd);
-    if (rc == ESP_OK) rc = run<3>(h->num_sms, h->stream, sink, imad);
-    cudaFree(sink);
-    return rc == ESP_OK ? ESP_OK : fail(h, rc, "integer peak probe failed");
+}  // namespace
+
+extern "C" int esp_probe_simd16_peaks(int device, double *addmax, double *max3) {
+    if (!addmax || !max3) return ESP_EINVAL;
+    const ProbeFn fns[2] = {run<4>, run<5>};
+    double *out[2] = {addmax, max3};
+    return run_probes(device, 2, fns, out);
+}
+
+extern "C" int esp_probe_int_peaks(int device, double *lop3, double *imnmx, double *iadd,
+                                   double *imad) {
+    if (!lop3 || !imnmx || !iadd || !imad) return ESP_EINVAL;
+    const ProbeFn fns[4] = {run<0>, run<1>, run<2>, run<3>};
+    double *out[4] = {lop3, imnmx, iadd, imad};
+    return run_probes(device, 4, fns, out);
 }

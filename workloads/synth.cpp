@@ -12,7 +12,7 @@
 #include <thread>
 #include <vector>
 
-#include "esperanto_gb300.h"
+#include "esp_workloads.h"
 
 namespace {
 
