@@ -165,7 +165,8 @@ def lib():
                                                                    C.c_void_p]
         L.orc_batch_myers_best_end.restype = i64
         L.orc_batch_channel_a.argtypes = [C.c_void_p] * 13 + [i64, C.c_int, C.c_void_p,
-                                                               C.c_void_p, C.c_void_p]
+                                                               C.c_void_p, C.c_void_p,
+                                                               C.c_void_p]
         L.free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -561,9 +562,19 @@ def batch_myers_best_end(seqs, read_off, read_len, text_off, text_len, threads: 
     return int(cells), dist, end
 
 
-def batch_channel_a(garena, contigs, read_ascii, read_off, reads, cands, threads: int):
+class _CaDetail(C.Structure):
+    _fields_ = [("cand", C.c_void_p), ("dro", C.c_void_p), ("pos", C.c_void_p),
+                ("signal", C.c_void_p), ("n_ops", C.c_void_p), ("ops", C.c_void_p),
+                ("ops_stride", C.c_uint32)]
+
+
+def batch_channel_a(garena, contigs, read_ascii, read_off, reads, cands, threads: int,
+                    ops_stride: int = 0):
     """Channel A per read with `threads` workers (plus strand, defaults).
-    Returns (found, score, dp_cells)."""
+    Returns (found, score, dp_cells), or with ops_stride > 0
+    (found, score, dp_cells, detail) where detail holds per read the winning
+    candidate (-1 when none), dro, pos, signal, n_ops and the spliced CIGAR
+    (first ops_stride ops)."""
     import numpy as np
     n = len(reads)
     keep = [np.ascontiguousarray(a) for a in (
@@ -576,10 +587,20 @@ def batch_channel_a(garena, contigs, read_ascii, read_off, reads, cands, threads
     found = np.zeros(n, np.int32)
     score = np.zeros(n, np.int32)
     cells = C.c_int64()
+    det = None
+    if ops_stride:
+        det = dict(cand=np.zeros(n, np.int32), dro=np.zeros(n, np.uint32),
+                   pos=np.zeros(n, np.uint32), signal=np.zeros(n, np.int32),
+                   n_ops=np.zeros(n, np.uint32), ops=np.zeros((n, ops_stride), np.uint32))
+        d = _CaDetail(*[det[k].ctypes.data for k in ("cand", "dro", "pos", "signal", "n_ops",
+                                                      "ops")], ops_stride)
     rc = lib().orc_batch_channel_a(*[a.ctypes.data for a in keep], n, threads,
-                                   found.ctypes.data, score.ctypes.data, C.byref(cells))
+                                   found.ctypes.data, score.ctypes.data, C.byref(cells),
+                                   C.byref(d) if det is not None else None)
     if rc != 0:
         raise OracleError(f"orc_batch_channel_a returned {rc}")
+    if det is not None:
+        return found, score, cells.value, det
     return found, score, cells.value
 
 

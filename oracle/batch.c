@@ -192,6 +192,7 @@ typedef struct {
     int32_t *found, *score;
     int rc;
     int64_t cells;
+    orc_ca_detail *det;         /* optional per-read detail (NULL: none) */
 } ca_job;
 
 static void *ca_worker(void *arg) {
@@ -217,6 +218,18 @@ static void *ca_worker(void *arg) {
         if (rc != ORC_OK) { jb->rc = rc; break; }
         jb->found[r] = out.found;
         jb->score[r] = out.score;
+        orc_ca_detail *d = jb->det;
+        if (d) {
+            d->cand[r] = out.found ? out.cand : -1;
+            d->dro[r] = out.dro;
+            d->pos[r] = out.pos;
+            d->signal[r] = out.signal;
+            d->n_ops[r] = out.found ? out.n_ops : 0;
+            if (out.found && d->ops) {
+                uint32_t c = out.n_ops < d->ops_stride ? out.n_ops : d->ops_stride;
+                memcpy(d->ops + (size_t)r * d->ops_stride, ops, c * sizeof(uint32_t));
+            }
+        }
     }
     jb->cells = orc_tls_cells - c0;
     return NULL;
@@ -228,7 +241,7 @@ int orc_batch_channel_a(const uint8_t *garena, const uint64_t *cbase, const uint
                         const uint32_t *cand_first, const uint32_t *cand_count,
                         const uint32_t *cstart, const uint32_t *cend, const uint32_t *csupport,
                         int64_t n_reads, int threads, int32_t *found, int32_t *score,
-                        int64_t *cells) {
+                        int64_t *cells, orc_ca_detail *detail) {
     if (threads < 1) threads = 1;
     if (threads > 1024) threads = 1024;
     pthread_t *tid = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
@@ -239,7 +252,7 @@ int orc_batch_channel_a(const uint8_t *garena, const uint64_t *cbase, const uint
         ca_job *jb = &jobs[t];
         *jb = (ca_job){garena, cbase, clen, reads, read_off, read_len, tail_start, contig,
                        cand_first, cand_count, cstart, cend, csupport, 0, 0, found, score, 0,
-                       0};
+                       0, detail};
         jb->lo = (int64_t)t * chunk;
         jb->hi = jb->lo + chunk < n_reads ? jb->lo + chunk : n_reads;
         if (jb->lo > jb->hi) jb->lo = jb->hi;

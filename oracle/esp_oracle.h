@@ -219,13 +219,24 @@ int64_t orc_batch_myers_best_end(const uint8_t *seqs, const uint64_t *read_off,
 
 /* Channel A over many reads (plus strand, default parameters), one contig
  * per read given by (cbase, clen) into a 2-bit arena without N. */
+/* Optional per-read detail of orc_batch_channel_a: the winning candidate
+ * (-1 when none), breakpoint, position, signal and the spliced CIGAR (the
+ * first ops_stride ops per read; ops may be NULL). */
+typedef struct {
+    int32_t *cand;
+    uint32_t *dro, *pos;
+    int32_t *signal;
+    uint32_t *n_ops;
+    uint32_t *ops;
+    uint32_t ops_stride;
+} orc_ca_detail;
 int orc_batch_channel_a(const uint8_t *garena, const uint64_t *cbase, const uint32_t *clen,
                         const uint8_t *reads, const uint64_t *read_off, const uint32_t *read_len,
                         const uint32_t *tail_start, const uint32_t *contig,
                         const uint32_t *cand_first, const uint32_t *cand_count,
                         const uint32_t *cstart, const uint32_t *cend, const uint32_t *csupport,
                         int64_t n_reads, int threads, int32_t *found, int32_t *score,
-                        int64_t *cells);
+                        int64_t *cells, orc_ca_detail *detail);
 
 #ifdef __cplusplus
 }
