@@ -458,16 +458,17 @@ class SpliceWorkload(Workload):
         return run, f"{sample} split reads of the same workload per step"
 
 
-def serve_bench(args):
-    """The serving workload: the serving loop on a 3.1-Gbp resident genome.  Measures the
-    saturated throughput (closed loop), then Poisson arrivals of 1k-64k-read
-    requests (log-uniform) at 70% and 80% of it, reporting p50/p99 latency."""
-    import torch
+def serve_phase(args, device=0, clocked=True):
+    """The serving workload: the serving loop on a resident synthetic genome
+    (3.1 Gbp by default).  Measures the saturated throughput (closed loop),
+    then Poisson arrivals of 1k-64k-read requests (log-uniform) at 70% and
+    80% of it, reporting p50/p99 latency, with nvidia-smi clock samples over
+    the loaded phases, the integer roofline at peak and the oracle's
+    extend_hint on the same kind of reads as the CPU baseline."""
     from esperanto_gb300 import serve as SV
     from esperanto_gb300.extend import ExtendBuffer
     from esperanto_gb300.split import Genome
-    torch.cuda.set_device(0)
-    buf = ExtendBuffer(0)
+    buf = ExtendBuffer(device)
     t0 = time.perf_counter()
     garena, contigs = W.synth_genome(5, args.genome_bases, 24)
     genome = Genome(garena, contigs, buf=buf)
@@ -475,11 +476,16 @@ def serve_bench(args):
     rng = np.random.default_rng(5)
     sizes = np.exp(rng.uniform(np.log(1000), np.log(65536), args.pool)).astype(int)
     pool = [W.synth_request(5, k, garena, contigs, int(n)) for k, n in enumerate(sizes)]
-    srv = SV.Server(genome, n_streams=args.streams, max_reads=65536, mem_budget=16 << 30)
+    srv = SV.Server(genome, n_streams=args.streams, max_reads=65536, mem_budget=16 << 30,
+                    device=device)
     # warm up every slot
     for t in [srv.submit(*pool[k % len(pool)]) for k in range(2 * args.streams)]:
         srv.wait(t)
-    lat, pairs, wall, tks = SV.run_load(srv, pool, 0, args.serve_seconds / 2, closed_loop=True)
+    clk = ClockSampler()
+    if clocked:
+        clk.start()
+    peak_s = max(1.0, args.serve_seconds / 2)
+    lat, pairs, wall, tks = SV.run_load(srv, pool, 0, peak_s, closed_loop=True)
     peak = pairs / wall
     cells = sum(SV.hint_cells(t.reads, contigs, t.out) for t in tks)
     peak_gcups = cells / wall / 1e9
@@ -490,17 +496,73 @@ def serve_bench(args):
             "offered_pairs_per_s": frac * peak, "achieved_pairs_per_s": pairs / wall,
             "requests": len(lat), "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max())}
+    clocks = clk.stop(device) if clocked else None
     srv.destroy()
-    r70 = res["70pct"]
+    out = {"workload": "serve loop: %.2f-Gbp resident genome (24 contigs), Poisson requests of "
+                       "1k-64k reads (log-uniform), 2x150 PE, windows read +- 32, extend_hint "
+                       "policy" % (args.genome_bases / 1e9),
+           "streams": args.streams, "request_pool": args.pool,
+           "peak_pairs_per_s": peak, "peak_gcups": peak_gcups, "peak_seconds": peak_s,
+           "load": res, "load_seconds": args.serve_seconds, "setup_s": setup_s,
+           "clocks": clocks}
+    if clocked:
+        peak_ops, _ = int_peak(device, 1)
+        out["roofline"] = {"bound": "int_alu",
+                           "achieved": peak_gcups * 1e9 * OPS_PER_CELL / 1e12,
+                           "peak": peak_ops / 1e12, "unit": "Tops/s",
+                           "frac": peak_gcups * 1e9 * OPS_PER_CELL / peak_ops,
+                           "note": "saturated serve throughput (one pair per thread kernel)"}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = serve_cpu_baseline(garena, contigs, pool[0])
+    return out
+
+
+def serve_cpu_baseline(garena, contigs, request):
+    """The oracle's extend_hint (the reference's scalar path) over one
+    served request's reads on all host cores: GCUPS and pairs/s."""
+    import oracle as O
+    from esperanto_gb300 import batch as B
+    from esperanto_gb300 import serve as SV
+    arena, reads = request
+    pairs = SV.serve_pairs(reads, contigs)
+    idx = np.arange(len(reads))
+    win_lo = int(pairs["win_pos"].min())
+    win_hi = int((pairs["win_pos"] + pairs["win_len"]).max())
+    # the reads, then the genome span their windows fall in, as one ASCII run
+    rseq = B._ASCII[B.unpack_codes(arena, 0, len(reads) * 150)]
+    gseq = B._ASCII[B.unpack_codes(garena, win_lo, win_hi - win_lo)]
+    seq = np.concatenate([rseq, gseq])
+    threads = os.cpu_count() or 1
+
+    def run():
+        t = time.perf_counter()
+        cells, _ = O.batch_extend(seq, pairs["read_pos"][idx], pairs["read_len"][idx],
+                                  pairs["win_pos"][idx] - win_lo + len(rseq),
+                                  pairs["win_len"][idx], pairs["band_offset"][idx],
+                                  pairs["band_half"][idx], O.Params(), 1, threads)
+        return cells, time.perf_counter() - t
+    run()
+    cells, dt = run()
+    return {"value": cells / dt / 1e9, "unit": "GCUPS", "pairs_per_s": len(idx) / dt,
+            "cores": threads, "kind": "port",
+            "sample": f"one served request of {len(idx)} reads through the oracle's "
+                      "extend_hint (the reference's scalar code path on aarch64)"}
+
+
+def serve_bench(args):
+    """--config 4: the serve phase alone, as its own JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    sv = serve_phase(args, 0)
+    r70 = sv["load"]["70pct"]
     line = {"metric": "serve p99 latency at 70% of peak load", "value": r70["p99_ms"],
             "unit": "ms", "n_gpus": 1, "higher_is_better": False, "data": "synthetic",
             "dtype": "int16", "vs_baseline": None,
-            "config": {"workload": "serve loop: %.2f-Gbp resident genome (24 contigs), Poisson "
-                                   "requests of 1k-64k reads (log-uniform), 2x150 PE, windows "
-                                   "read +- 32, extend_hint policy" % (args.genome_bases / 1e9),
-                       "streams": args.streams, "request_pool": args.pool},
-            "peak_pairs_per_s": peak, "peak_gcups": peak_gcups, "load": res,
-            "setup_s": setup_s}
+            "config": {"workload": sv["workload"], "streams": args.streams,
+                       "request_pool": args.pool},
+            "peak_pairs_per_s": sv["peak_pairs_per_s"], "peak_gcups": sv["peak_gcups"],
+            "load": sv["load"], "setup_s": sv["setup_s"], "clocks": sv["clocks"],
+            "roofline": sv.get("roofline"), "cpu_baseline": sv.get("cpu_baseline")}
     print(json.dumps(line), flush=True)
 
 
@@ -569,7 +631,10 @@ def main():
     ap.add_argument("--genome-bases", type=int, default=3_100_000_000)
     ap.add_argument("--pool", type=int, default=48)
     ap.add_argument("--streams", type=int, default=4)
-    ap.add_argument("--serve-seconds", type=float, default=12.0)
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
+                    help="seconds at each of 70%% and 80%% of peak in the serve phase")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the serve phase of the default (mixed-length) line")
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--e2e-steps", type=int, default=8)
@@ -722,10 +787,15 @@ def main():
     if config == 3:
         line["config"]["candidates"] = wl.n_cands
         line["config"]["rescued"] = wl.found
-    if config == 0:
-        # the same pairs through extend_hint: its escalation rate is the
-        # measure of how often the reference's two-attempt policy runs twice
+    if config in (0, 2):
+        # the same pairs through extend_hint, the policy the reference's
+        # callers run (align.rs:1907): its escalation rate is how often the
+        # two-attempt policy runs twice
         line["extend_hint"] = wl.hint_measure(buf, torch, stream)
+    if config == 2 and not args.no_serve and world == 1:
+        # the serving loop (continuous batching over a resident genome),
+        # with its own clock record
+        line["serve"] = serve_phase(args, local)
     print(json.dumps(line), flush=True)
 
 
