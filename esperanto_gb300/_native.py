@@ -99,6 +99,12 @@ class ServerConfigC(C.Structure):
                 ("mem_budget_bytes", C.c_uint64)]
 
 
+class ServerStatsC(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("launches", "reads", "merged_launches",
+                                          "split_requests", "budget_waits", "cut_launches",
+                                          "pool_bytes", "pool_peak_bytes")]
+
+
 class BatchLimitsC(C.Structure):
     _fields_ = [("max_read_len", C.c_uint32), ("max_win_len", C.c_uint32),
                 ("max_half", C.c_int32)]
@@ -198,6 +204,7 @@ def lib():
     L.esp_server_submit.argtypes = [vp, C.POINTER(ServeRequestC), C.POINTER(C.c_uint64)]
     L.esp_server_wait.argtypes = [vp, C.c_uint64, C.c_int, C.POINTER(C.c_int32),
                                   C.POINTER(C.c_double)]
+    L.esp_server_get_stats.argtypes = [vp, C.POINTER(ServerStatsC)]
     L.esp_server_close.argtypes = [vp]
     L.esp_server_destroy.argtypes = [vp]
     L.esp_last_cells.argtypes = [vp]

@@ -70,6 +70,102 @@ static bool band_paired(esp_handle *h, uint64_t n) {
     return esp::gotoh_paired(band_variant(h, n));
 }
 
+// How one batch of n_pairs uses DP scratch: which kernel runs, with how
+// many warps, and the traceback / row-buffer bytes they need (the choices
+// enqueue_batch makes; the serve loop charges launches with it).
+struct DpPlan {
+    bool warp_kernel = false;
+    int var = 1;             // thread-kernel variant
+    bool per_class = false;  // one launch per length class of the binned list
+    bool paired = false;     // a two-pairs-per-thread variant is among the launches
+    uint64_t warps = 0;
+    uint64_t tbw = 0, rbw = 0;  // words per thread (warp kernel: per warp)
+    uint64_t tb_bytes = 0, rb_bytes = 0;
+};
+
+static DpPlan plan_dp(esp_handle *h, int mode, uint64_t n_pairs, const Limits &L1,
+                      const Limits &L2) {
+    DpPlan P;
+    if (h->warp_max < 0) {
+        const char *v = getenv("ESP_WARP_MAX");
+        h->warp_max = v ? atol(v) : 2048;
+    }
+    P.tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
+    P.rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
+    if (n_pairs <= (uint64_t)h->warp_max) {
+        // Few pairs: one warp per pair (the wavefront kernel), so a lone
+        // pair is not latency-bound on a single thread.
+        P.warp_kernel = true;
+        uint64_t per_warp_bytes = (P.tbw + P.rbw) * 4;
+        uint64_t warps = std::min<uint64_t>(n_pairs, (uint64_t)h->num_sms * 12);
+        warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes));
+        P.warps = (warps + 3) / 4 * 4;  // whole blocks: every launched warp owns its scratch
+        P.tb_bytes = P.warps * per_warp_bytes;
+        return P;
+    }
+    // scratch slots: one warp per 32 pairs up to the resident limit, bounded
+    // by the scratch budget
+    uint64_t per_warp_bytes = (P.tbw + P.rbw) * 32 * 4;
+    resolve_variant(h);
+    // the paired kernels need neighbours of the binned list with one band
+    // geometry
+    auto usable = [&](int v) {
+        return esp::gotoh_paired(v) && (mode != ESP_MODE_BAND || !h->binning) ? v - 2 : v;
+    };
+    int var = mode == ESP_MODE_HINT ? hint_variant(h, n_pairs) : usable(band_variant(h, n_pairs));
+    // autotuned handle: one variant for every class runs as a single launch
+    bool tuned_split = false;
+    if (h->tuned && mode == ESP_MODE_BAND) {
+        for (int s = 1; s < esp::kLengthClasses; s++) tuned_split |= h->tune[s] != h->tune[0];
+        if (!tuned_split && h->tune[0] >= 0) var = usable(h->tune[0]);
+    }
+    // the binned list runs per length class when the handle is autotuned (or
+    // is being tuned); scratch then covers the widest variant in use
+    P.per_class = (tuned_split || h->autotune_ms) && h->binning && n_pairs > 32;
+    int max_bps = 0;
+    for (int v = 0; v < esp::kGotohVariants; v++) {
+        bool used = v == var;
+        if (P.per_class)
+            for (int s = 0; s < esp::kLengthClasses; s++) used |= h->autotune_ms || h->tune[s] == v;
+        if (!used) continue;
+        if (h->gotoh_bps[v] == 0) h->gotoh_bps[v] = esp::gotoh_blocks_per_sm(128, v);
+        max_bps = std::max(max_bps, h->gotoh_bps[v]);
+        P.paired |= esp::gotoh_paired(v);
+    }
+    P.var = var;
+    const uint64_t slot_pairs = P.paired ? 2 : 1;  // scratch slots per lane
+    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * max_bps * 4);
+    uint64_t need_warps = (n_pairs + 31) / 32;
+    uint64_t warps = std::min(want, need_warps);
+    uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / (per_warp_bytes * slot_pairs));
+    warps = std::min(warps, budget_warps);
+    P.warps = (warps + 3) / 4 * 4;  // whole 128-thread blocks: every launched warp owns a slot
+    P.tb_bytes = P.warps * slot_pairs * P.tbw * 32 * 4;
+    P.rb_bytes = P.warps * slot_pairs * P.rbw * 32 * 4;
+    return P;
+}
+
+void dp_scratch_bytes(esp_handle *h, int mode, uint64_t n_pairs, const Limits &L1,
+                      const Limits &L2, uint64_t &tb_bytes, uint64_t &rb_bytes) {
+    const DpPlan P = plan_dp(h, mode, n_pairs, L1, L2);
+    tb_bytes = P.tb_bytes;
+    rb_bytes = P.rb_bytes;
+}
+
+// The traceback and row-buffer scratch of a plan: grown in the handle, or
+// checked against the region the owner placed there (scratch_external).
+static int scratch_for(esp_handle *h, const DpPlan &P) {
+    if (h->scratch_external) {
+        if (P.tb_bytes > h->d_tb_cap || P.rb_bytes > h->d_rb_cap)
+            return fail(h, ESP_ENOMEM, "DP scratch region too small for the launch");
+        return ESP_OK;
+    }
+    int rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, P.tb_bytes);
+    if (rc == ESP_OK && P.rb_bytes)
+        rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, P.rb_bytes);
+    return rc;
+}
+
 // Enqueue the DP launches of one batch whose inputs are on the device.
 int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_pairs,
                   const uint8_t *d_arena, uint64_t arena_bytes, const esp_n_interval *d_iv,
@@ -81,21 +177,9 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     // list positions are u32, with up to 2^20 padding slots
     if (n_pairs > 0xffffffffull - (1ull << 21)) return fail(h, ESP_EINVAL, "batch too large");
     int rc;
-    if (h->warp_max < 0) {
-        const char *v = getenv("ESP_WARP_MAX");
-        h->warp_max = v ? atol(v) : 2048;
-    }
-    if (n_pairs <= (uint64_t)h->warp_max) {
-        // Few pairs: one warp per pair (the wavefront kernel), so a lone
-        // pair is not latency-bound on a single thread.
-        uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
-        uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
-        uint64_t per_warp_bytes = (tbw + rbw) * 4;
-        uint64_t warps = std::min<uint64_t>(n_pairs, (uint64_t)h->num_sms * 12);
-        warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / per_warp_bytes));
-        warps = (warps + 3) / 4 * 4;  // whole blocks: every launched warp owns its scratch
-        if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * per_warp_bytes)) != ESP_OK)
-            return rc;
+    const DpPlan P = plan_dp(h, mode, n_pairs, L1, L2);
+    if ((rc = scratch_for(h, P)) != ESP_OK) return rc;
+    if (P.warp_kernel) {
         if (mode == ESP_MODE_HINT &&
             (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
             return rc;
@@ -113,66 +197,26 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         job.cigar = d_cigar;
         job.cigar_stride = cigar_stride;
         job.tb = h->d_tb;
-        job.tb_words = tbw;
-        job.rb_words = rbw;
+        job.tb_words = P.tbw;
+        job.rb_words = P.rbw;
         job.esc_list = h->d_esc;
         job.esc_count = h->d_ctr + 4;
         job.mode = mode == ESP_MODE_HINT ? 1 : 0;
-        CK(h, esp::launch_gotoh_warp(job, K, (int)warps, st));
+        CK(h, esp::launch_gotoh_warp(job, K, (int)P.warps, st));
         h->launches++;
         if (mode == ESP_MODE_HINT) {
             esp::GotohJob j2 = job;
             j2.mode = 2;
             j2.list = h->d_esc;
             j2.list_count = h->d_ctr + 4;
-            CK(h, esp::launch_gotoh_warp(j2, K, (int)warps, st));
+            CK(h, esp::launch_gotoh_warp(j2, K, (int)P.warps, st));
             h->launches++;
         }
         return ESP_OK;
     }
-    // scratch slots: one warp per 32 pairs up to the resident limit, bounded
-    // by the scratch budget
-    uint64_t tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
-    uint64_t rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
-    uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    resolve_variant(h);
-    // the paired kernels need neighbours of the binned list with one band
-    // geometry
-    auto usable = [&](int v) {
-        return esp::gotoh_paired(v) && (mode != ESP_MODE_BAND || !h->binning) ? v - 2 : v;
-    };
-    int var = mode == ESP_MODE_HINT ? hint_variant(h, n_pairs) : usable(band_variant(h, n_pairs));
-    // autotuned handle: one variant for every class runs as a single launch
-    bool tuned_split = false;
-    if (h->tuned && mode == ESP_MODE_BAND) {
-        for (int s = 1; s < esp::kLengthClasses; s++) tuned_split |= h->tune[s] != h->tune[0];
-        if (!tuned_split && h->tune[0] >= 0) var = usable(h->tune[0]);
-    }
-    // the binned list runs per length class when the handle is autotuned (or
-    // is being tuned); scratch then covers the widest variant in use
-    const bool per_class = (tuned_split || h->autotune_ms) && h->binning && n_pairs > 32;
-    int max_bps = 0;
-    bool paired = false;
-    for (int v = 0; v < esp::kGotohVariants; v++) {
-        bool used = v == var;
-        if (per_class)
-            for (int s = 0; s < esp::kLengthClasses; s++) used |= h->autotune_ms || h->tune[s] == v;
-        if (!used) continue;
-        if (h->gotoh_bps[v] == 0) h->gotoh_bps[v] = esp::gotoh_blocks_per_sm(128, v);
-        max_bps = std::max(max_bps, h->gotoh_bps[v]);
-        paired |= esp::gotoh_paired(v);
-    }
-    const uint64_t slot_pairs = paired ? 2 : 1;  // scratch slots per lane
-    uint64_t want = std::max<uint64_t>(1, (uint64_t)h->num_sms * max_bps * 4);
-    uint64_t need_warps = (n_pairs + 31) / 32;
-    uint64_t warps = std::min(want, need_warps);
-    uint64_t budget_warps = std::max<uint64_t>(1, h->scratch_budget / (per_warp_bytes * slot_pairs));
-    warps = std::min(warps, budget_warps);
-    warps = (warps + 3) / 4 * 4;  // whole 128-thread blocks: every launched warp owns a slot
-    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * slot_pairs * tbw * 32 * 4)) != ESP_OK)
-        return rc;
-    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * slot_pairs * rbw * 32 * 4)) != ESP_OK)
-        return rc;
+    const uint64_t tbw = P.tbw, rbw = P.rbw, warps = P.warps;
+    const int var = P.var;
+    const bool per_class = P.per_class, paired = P.paired;
     if (mode == ESP_MODE_HINT &&
         (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
         return rc;
@@ -270,25 +314,8 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
 
 
 
-int reserve_dp(esp_handle *h, uint64_t max_pairs, uint32_t max_m, uint32_t max_n) {
-    Limits L1, L2;
-    add_limits(L1, max_m, max_n, 30);
-    add_limits(L2, max_m, max_n, -1);
-    uint64_t tbw = std::max(L1.tb_words, L2.tb_words), rbw = std::max(L1.rb_words, L2.rb_words);
-    uint64_t per_warp_bytes = (tbw + rbw) * 32 * 4;
-    resolve_variant(h);
-    if (h->gotoh_bps[h->variant] == 0)
-        h->gotoh_bps[h->variant] = esp::gotoh_blocks_per_sm(128, h->variant);
-    const uint64_t slot_pairs = esp::gotoh_paired(h->variant) ? 2 : 1;
-    uint64_t warps = std::min<uint64_t>((uint64_t)h->num_sms * h->gotoh_bps[h->variant] * 4,
-                                        (max_pairs + 31) / 32);
-    warps = std::min(warps, std::max<uint64_t>(1, h->scratch_budget / (per_warp_bytes * slot_pairs)));
-    warps = (warps + 3) / 4 * 4;
+int reserve_lists(esp_handle *h, uint64_t max_pairs) {
     int rc;
-    if ((rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, warps * slot_pairs * tbw * 32 * 4)) != ESP_OK)
-        return rc;
-    if ((rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, warps * slot_pairs * rbw * 32 * 4)) != ESP_OK)
-        return rc;
     if ((rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, max_pairs * 4)) != ESP_OK) return rc;
     if ((rc = grow_device(h, (void **)&h->d_hist, &h->d_hist_cap, esp::bin_scratch_bytes())) != ESP_OK)
         return rc;
@@ -338,8 +365,10 @@ int esp_destroy(esp_handle *h) {
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     cudaFree(h->d_in);
     cudaFree(h->d_res);
-    cudaFree(h->d_tb);
-    cudaFree(h->d_rb);
+    if (!h->scratch_external) {
+        cudaFree(h->d_tb);
+        cudaFree(h->d_rb);
+    }
     cudaFree(h->d_esc);
     cudaFree(h->d_ctr);
     cudaFree(h->d_bat);

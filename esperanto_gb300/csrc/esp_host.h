@@ -39,13 +39,16 @@ struct esp_handle {
     uint64_t graph_launches = 0;
     int use_graphs = -1;  // -1 = ESP_GRAPHS env (default on)
     uint64_t scratch_budget = 8ull << 30;  // bytes of DP scratch one launch may use
+    // d_tb / d_rb (with their caps) are a region the owner placed there, not
+    // the handle's own: launches check them instead of growing them
+    bool scratch_external = false;
     // grow-only device buffers
     void *d_in = nullptr;       // per-call staging: pair | n intervals | arena
     size_t d_in_cap = 0;
     void *d_res = nullptr;      // per-call results: esp_extension | cigar
     size_t d_res_cap = 0;
     uint32_t *d_tb = nullptr;
-    size_t d_tb_cap = 0;        // words
+    size_t d_tb_cap = 0;        // bytes
     uint32_t *d_rb = nullptr;
     size_t d_rb_cap = 0;
     uint32_t *d_esc = nullptr;  // escalation list
@@ -205,6 +208,12 @@ struct esp_genome {
     std::vector<esp_n_interval> h_iv;  // host copy (serve-loop window clipping)
 };
 
-// Grow a handle's DP scratch once for batches of up to max_pairs pairs of
-// at most max_m x max_n in extend_hint mode (abi.cu).
-int reserve_dp(esp_handle *h, uint64_t max_pairs, uint32_t max_m, uint32_t max_n);
+// Bytes of traceback and row-buffer scratch one enqueue_batch of n_pairs
+// uses on this handle (the kernel, warps and words it would choose; abi.cu).
+void dp_scratch_bytes(esp_handle *h, int mode, uint64_t n_pairs, const Limits &L1,
+                      const Limits &L2, uint64_t &tb_bytes, uint64_t &rb_bytes);
+
+// Grow a handle's escalation and binning lists once for one-pair-kernel
+// batches of up to max_pairs pairs (abi.cu), so later batches of that size
+// allocate nothing but their DP scratch.
+int reserve_lists(esp_handle *h, uint64_t max_pairs);

@@ -2,9 +2,11 @@
 resident genome, behind the native server of csrc/serve.cpp.
 
 ``Server.submit`` hands a request (reads + their candidate windows) to the
-native worker thread and returns at once; the worker admits requests FIFO to
-idle CUDA streams while the device-memory budget allows, so requests that
-arrive while others run overlap on the device.  ``Server.wait`` returns the
+native worker thread and returns at once; the worker turns the head of the
+FIFO queue into launches of up to ``max_reads`` reads (small requests share
+a launch, large ones run over several), each charged its DP scratch from one
+pool of ``mem_budget`` bytes, so requests that arrive while others run
+overlap on the device as slots and memory free up.  ``Server.wait`` returns the
 request's status and its submit-to-results latency.  ``run_load`` drives a
 server with Poisson arrivals for the serve benchmark.
 """
@@ -78,6 +80,14 @@ class Server:
         if rc:
             raise N.EspError(rc, "esp_server_wait")
         return st.value, lat.value
+
+    def stats(self) -> dict:
+        """Admission and memory counters since creation (esp_server_stats)."""
+        st = N.ServerStatsC()
+        rc = N.lib().esp_server_get_stats(self._s, C.byref(st))
+        if rc:
+            raise N.EspError(rc, "esp_server_get_stats")
+        return {k: getattr(st, k) for k, _ in N.ServerStatsC._fields_}
 
     def close(self):
         N.lib().esp_server_close(self._s)

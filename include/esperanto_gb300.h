@@ -509,15 +509,20 @@ int esp_batch_rescore_host(esp_handle *h, const esp_genome *g, const esp_rescore
 
 /* ---- serving loop (new): continuous batching over a resident genome ----
  *
- * A server owns `n_streams` in-flight slots, each a CUDA stream with its own
- * pre-sized DP scratch.  Submitted requests wait in a FIFO; a native worker
- * thread admits the head request to an idle slot as soon as the slot and the
- * device-memory budget (DP scratch, dominated by traceback words) allow,
- * builds each read's candidate window from the resident genome, runs the
- * extend_hint policy on the slot's stream and copies results back, so
- * requests that arrive while others run are admitted as slots free up and
- * their work overlaps on the device.  Results of a request do not depend on
- * what else is in flight. */
+ * Submitted requests queue FIFO.  A native worker thread turns the head of
+ * the queue into DP launches of up to max_reads reads: small requests of
+ * one CIGAR stride that wait together share a launch, and a request larger
+ * than max_reads runs over several.  Each launch is charged the DP scratch
+ * it needs (traceback words of the extend_hint policy's full-matrix attempt
+ * for its longest read and window) from one device pool of
+ * mem_budget_bytes shared by all in-flight slots: a launch that does not fit
+ * is cut to the reads that do (at least 1,024), and when not even that fits
+ * the head request waits until a running launch returns its scratch.  Each
+ * read's candidate window is read in place from the resident genome, the
+ * extend_hint policy runs on the slot's stream and results are copied back,
+ * so requests that arrive while others run are admitted as slots and memory
+ * free up, and their work overlaps on the device.  Results of a request do
+ * not depend on what else is in flight. */
 typedef struct {
     uint64_t read_pos;     /* base offset in the request's read arena */
     uint32_t read_len;
@@ -539,26 +544,40 @@ typedef struct {
 } esp_serve_request;
 
 typedef struct {
-    uint32_t n_streams;        /* in-flight slots (default 4) */
-    uint32_t max_reads;        /* largest request accepted (default 131072) */
+    uint32_t n_streams;        /* in-flight launch slots (default 4, at most 64) */
+    uint32_t max_reads;        /* reads per launch (default 131072, below 2^20) */
     uint32_t max_read_len;     /* default 300 */
     uint32_t max_win_len;      /* default max_read_len + 128 */
-    uint64_t mem_budget_bytes; /* device scratch admitted at once (default 16 GiB) */
+    uint64_t mem_budget_bytes; /* the DP scratch pool, allocated at creation (default 16 GiB) */
 } esp_server_config;
+
+typedef struct {
+    uint64_t launches;         /* DP launches completed */
+    uint64_t reads;            /* reads in them */
+    uint64_t merged_launches;  /* launches holding reads of more than one request */
+    uint64_t split_requests;   /* requests whose reads ran in more than one launch */
+    uint64_t budget_waits;     /* requests held at the head of the queue for scratch memory */
+    uint64_t cut_launches;     /* launches cut short to fit the free scratch */
+    uint64_t pool_bytes;       /* the scratch pool (the memory budget) */
+    uint64_t pool_peak_bytes;  /* most of it charged at once */
+} esp_server_stats;
 
 typedef struct esp_server esp_server;
 
 int esp_server_create(esp_genome *g, const esp_extend_params *params,
                       const esp_server_config *cfg, int device, esp_server **out);
-/* Non-blocking.  ESP_EBUSY: the request alone exceeds the memory budget or
- * max_reads; ESP_ECLOSED: the server is closing. */
+/* Non-blocking; requests of any size (cigar_stride at most 64).  ESP_EBUSY:
+ * even its smallest launch exceeds the whole memory budget; ESP_EINVAL: a
+ * read outside its limits or tables; ESP_ECLOSED: the server is closing. */
 int esp_server_submit(esp_server *s, const esp_serve_request *req, uint64_t *ticket);
 /* Wait (bounded) for a ticket: ESP_OK with *status the request's status and
  * *latency_ms submit-to-results time, or ESP_ETIMEOUT. */
 int esp_server_wait(esp_server *s, uint64_t ticket, int timeout_ms, int32_t *status,
                     double *latency_ms);
-/* Stop admitting: pending (not yet admitted) requests complete with
- * ESP_ECLOSED; in-flight ones finish normally. */
+/* Admission and memory counters since creation. */
+int esp_server_get_stats(esp_server *s, esp_server_stats *out);
+/* Stop admitting: queued requests none of whose reads has started complete
+ * with ESP_ECLOSED; started ones finish normally. */
 int esp_server_close(esp_server *s);
 int esp_server_destroy(esp_server *s);
 

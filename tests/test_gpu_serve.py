@@ -70,11 +70,92 @@ def test_alone_equals_mix_equals_batch_and_oracle(setup):
         assert O.extend_hint(r, w, O.Params(), offset=int(pairs["band_offset"][k])).key() == ref[k]
 
 
+def _keys(t):
+    return [_key(t, k) for k in range(len(t.reads))]
+
+
+def test_large_requests_split_small_ones_share_launches(setup):
+    """A request of 60,000 reads on a server of 8,192-read launches runs
+    over several launches; ten small requests queued behind it share a
+    launch with its tail; every result equals the request run alone on the
+    module's server."""
+    garena, contigs, g, srv = setup
+    big = W.synth_request(5, 7, garena, contigs, 60000)
+    small = [W.synth_request(5, 500 + k, garena, contigs, 300 + 50 * k) for k in range(10)]
+    want = []
+    for a, r in [big] + small:
+        t = srv.submit(a, r)
+        assert srv.wait(t)[0] == 0
+        want.append(_keys(t))
+    s1 = SV.Server(g, n_streams=1, max_reads=8192, mem_budget=1 << 30)
+    try:
+        ts = [s1.submit(a, r) for a, r in [big] + small]
+        for t in ts:
+            assert s1.wait(t)[0] == 0
+        assert [_keys(t) for t in ts] == want
+        st = s1.stats()
+        assert st["split_requests"] >= 1 and st["merged_launches"] >= 1, st
+        assert st["reads"] == sum(len(r) for _, r in [big] + small)
+        assert st["launches"] >= 8
+    finally:
+        s1.destroy()
+
+
+def test_memory_budget_binds_before_slots(setup):
+    """Four slots but scratch for about one and a half launches: the second
+    launch is cut to the scratch left, later requests wait at the head of
+    the queue for scratch (not for a slot) and run when a launch returns its
+    share; the pool is never over-committed and every result equals the
+    ample-budget server's."""
+    garena, contigs, g, srv = setup
+    reqs = [W.synth_request(5, 600 + k, garena, contigs, 8192) for k in range(6)]
+    want = []
+    for a, r in reqs:
+        t = srv.submit(a, r)
+        assert srv.wait(t)[0] == 0
+        want.append(_keys(t))
+    # one 8,192-read launch of 150 x 214 extend_hint pairs charges 256 warps
+    # x 4,280 words x 32 lanes x 4 bytes = 140 MB
+    budget = 210 << 20
+    s2 = SV.Server(g, n_streams=4, max_reads=8192, mem_budget=budget)
+    try:
+        ts = [s2.submit(a, r) for a, r in reqs]
+        for t in ts:
+            assert s2.wait(t)[0] == 0
+        assert [_keys(t) for t in ts] == want
+        st = s2.stats()
+        assert st["budget_waits"] >= 1 and st["cut_launches"] >= 1, st
+        assert st["pool_bytes"] <= budget and st["pool_peak_bytes"] <= st["pool_bytes"], st
+        assert st["pool_peak_bytes"] > (140 << 20), st
+    finally:
+        s2.destroy()
+    # a request whose smallest launch cannot fit the budget is refused
+    s3 = SV.Server(g, n_streams=2, max_reads=8192, mem_budget=8 << 20)
+    try:
+        with pytest.raises(EspError) as ei:
+            s3.submit(*reqs[0])
+        assert ei.value.code == -6  # ESP_EBUSY
+    finally:
+        s3.destroy()
+
+
+def test_bounded_wait_times_out_then_completes(setup):
+    """esp_server_wait with a zero timeout on a request still in flight
+    returns ESP_ETIMEOUT and keeps the ticket; a later wait collects it."""
+    garena, contigs, g, srv = setup
+    t = srv.submit(*W.synth_request(5, 9, garena, contigs, 60000))
+    with pytest.raises(EspError) as ei:
+        srv.wait(t, 0)
+    assert ei.value.code == -7  # ESP_ETIMEOUT
+    st, lat = srv.wait(t, 60000)
+    assert st == 0 and lat > 0
+    # an empty request completes at once
+    a, r = W.synth_request(5, 10, garena, contigs, 10)
+    assert srv.wait(srv.submit(a, r[:0]), 1000)[0] == 0
+
+
 def test_admission_and_close(setup):
     garena, contigs, g, srv = setup
-    arena, reads = W.synth_request(5, 7, garena, contigs, 40000)  # > max_reads
-    with pytest.raises(EspError):
-        srv.submit(arena, reads)
     srv2 = SV.Server(g, n_streams=1, max_reads=32768, mem_budget=1 << 30)
     # requests are built first so that all six are queued within microseconds
     # and the single slot is still busy with the first when close() lands
