@@ -152,15 +152,17 @@ void dp_scratch_bytes(esp_handle *h, int mode, uint64_t n_pairs, const Limits &L
     rb_bytes = P.rb_bytes;
 }
 
-// The traceback and row-buffer scratch of a plan: grown in the handle, or
-// checked against the region the owner placed there (scratch_external).
-static int scratch_for(esp_handle *h, const DpPlan &P) {
+// The traceback and row-buffer scratch of a plan (tb at least tb_min
+// bytes): grown in the handle, or checked against the region the owner
+// placed there (scratch_external).
+static int scratch_for(esp_handle *h, const DpPlan &P, uint64_t tb_min) {
+    const uint64_t tb = std::max(P.tb_bytes, tb_min);
     if (h->scratch_external) {
-        if (P.tb_bytes > h->d_tb_cap || P.rb_bytes > h->d_rb_cap)
+        if (tb > h->d_tb_cap || P.rb_bytes > h->d_rb_cap)
             return fail(h, ESP_ENOMEM, "DP scratch region too small for the launch");
         return ESP_OK;
     }
-    int rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, P.tb_bytes);
+    int rc = grow_device(h, (void **)&h->d_tb, &h->d_tb_cap, tb);
     if (rc == ESP_OK && P.rb_bytes)
         rc = grow_device(h, (void **)&h->d_rb, &h->d_rb_cap, P.rb_bytes);
     return rc;
@@ -177,8 +179,50 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     // list positions are u32, with up to 2^20 padding slots
     if (n_pairs > 0xffffffffull - (1ull << 21)) return fail(h, ESP_EINVAL, "batch too large");
     int rc;
-    const DpPlan P = plan_dp(h, mode, n_pairs, L1, L2);
-    if ((rc = scratch_for(h, P)) != ESP_OK) return rc;
+    // Reads whose scores can leave the int16 domain: the int16 kernels list
+    // such pairs and the wide kernel runs them afterwards (int32, one warp
+    // per pair, both extend_hint attempts in-kernel), in the same scratch.
+    // The int16 kernels' scratch then covers reads up to K.max_m only.
+    const uint32_t max_m = std::max(L1.max_m, mode == ESP_MODE_HINT ? L2.max_m : 0u);
+    const bool wide = max_m > (uint32_t)K.max_m;
+    Limits N1 = L1, N2 = L2;
+    if (wide) {
+        const uint64_t strips = ((uint64_t)K.max_m + 7) / 8;
+        for (Limits *N : {&N1, &N2}) {
+            N->tb_words = std::min<uint64_t>(N->tb_words, strips * N->rb_words);
+            N->max_m = std::min<uint32_t>(N->max_m, (uint32_t)K.max_m);
+        }
+    }
+    const DpPlan P = plan_dp(h, mode, n_pairs, N1, N2);
+    uint64_t wide_warps = 0, wide_bytes = 0, wide_tbw = 0, wide_rbw = 0;
+    if (wide) {
+        wide_tbw = std::max(L1.tb_words, mode == ESP_MODE_HINT ? L2.tb_words : 0);
+        wide_rbw = std::max(L1.rb_words, mode == ESP_MODE_HINT ? L2.rb_words : 0);
+        const uint64_t per_warp = (wide_tbw + 2 * wide_rbw) * 4;
+        wide_warps = std::min<uint64_t>({n_pairs, (uint64_t)h->num_sms * 4,
+                                         std::max<uint64_t>(1, h->scratch_budget / per_warp)});
+        wide_warps = (wide_warps + 3) / 4 * 4;  // whole blocks: every warp owns its scratch
+        wide_bytes = wide_warps * per_warp;
+        if ((rc = grow_device(h, (void **)&h->d_wide, &h->d_wide_cap, n_pairs * 4)) != ESP_OK)
+            return rc;
+    }
+    if ((rc = scratch_for(h, P, wide_bytes)) != ESP_OK) return rc;
+    auto launch_wide = [&](const esp::GotohJob &base) -> int {
+        if (!wide) return ESP_OK;
+        esp::GotohJob jw = base;
+        jw.list = h->d_wide;
+        jw.list_count = h->d_ctr + 30;
+        jw.range = nullptr;
+        jw.mode = mode == ESP_MODE_HINT ? 1 : 0;
+        jw.tb = h->d_tb;
+        jw.tb_words = wide_tbw;
+        jw.rb_words = wide_rbw;
+        jw.wide_list = nullptr;
+        jw.wide_count = nullptr;
+        CK(h, esp::launch_gotoh_wide(jw, K, (int)wide_warps, st));
+        h->launches++;
+        return ESP_OK;
+    };
     if (P.warp_kernel) {
         if (mode == ESP_MODE_HINT &&
             (rc = grow_device(h, (void **)&h->d_esc, &h->d_esc_cap, n_pairs * sizeof(uint32_t))) != ESP_OK)
@@ -202,6 +246,8 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         job.esc_list = h->d_esc;
         job.esc_count = h->d_ctr + 4;
         job.mode = mode == ESP_MODE_HINT ? 1 : 0;
+        job.wide_list = wide ? h->d_wide : nullptr;
+        job.wide_count = h->d_ctr + 30;
         CK(h, esp::launch_gotoh_warp(job, K, (int)P.warps, st));
         h->launches++;
         if (mode == ESP_MODE_HINT) {
@@ -212,7 +258,7 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
             CK(h, esp::launch_gotoh_warp(j2, K, (int)P.warps, st));
             h->launches++;
         }
-        return ESP_OK;
+        return launch_wide(job);
     }
     const uint64_t tbw = P.tbw, rbw = P.rbw, warps = P.warps;
     const int var = P.var;
@@ -259,6 +305,8 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
     job.esc_list = h->d_esc;
     job.esc_count = h->d_ctr + 4;
     job.mode = mode == ESP_MODE_HINT ? 1 : 0;
+    job.wide_list = wide ? h->d_wide : nullptr;
+    job.wide_count = h->d_ctr + 30;
     if (per_class && h->autotune_ms) {
         // time every variant on every length class and, as row
         // kLengthClasses, on the whole list in one launch (best of two runs
@@ -276,6 +324,8 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
                         js.queue = h->d_ctr + 8 + 2 * s;
                     }
                     CK(h, cudaMemsetAsync(js.queue, 0, 8, st));
+                    // every timed run lists the wide pairs anew
+                    CK(h, cudaMemsetAsync(h->d_ctr + 30, 0, 4, st));
                     CK(h, cudaEventRecord(ev[0], st));
                     CK(h, esp::launch_gotoh(js, K, (int)warps, 128, st, v));
                     CK(h, cudaEventRecord(ev[1], st));
@@ -301,15 +351,26 @@ int enqueue_batch(esp_handle *h, int mode, const esp_pair *d_pairs, uint64_t n_p
         h->launches++;
     }
     if (mode == ESP_MODE_HINT) {
+        // extend_hint's second attempt (full matrix) over the escalations,
+        // binned by their full-matrix geometry like the first attempt's
+        // list (the first attempt is done with the binned list and its
+        // histogram by now)
         esp::GotohJob j2 = job;
         j2.mode = 2;
         j2.list = h->d_esc;
         j2.list_count = h->d_ctr + 4;
         j2.queue = h->d_ctr + 2;
+        if (order) {
+            CK(h, esp::launch_binning(d_pairs, n_pairs, 2, h->d_hist, h->d_order, h->num_sms, st,
+                                      h->d_ctr + 31, nullptr, paired, h->d_esc, h->d_ctr + 4));
+            h->launches += 5;
+            j2.list = h->d_order;
+            j2.list_count = paired ? h->d_ctr + 31 : h->d_ctr + 4;
+        }
         CK(h, esp::launch_gotoh(j2, K, (int)warps, 128, st, var));
         h->launches++;
     }
-    return ESP_OK;
+    return launch_wide(job);
 }
 
 
@@ -370,6 +431,7 @@ int esp_destroy(esp_handle *h) {
         cudaFree(h->d_rb);
     }
     cudaFree(h->d_esc);
+    cudaFree(h->d_wide);
     cudaFree(h->d_ctr);
     cudaFree(h->d_bat);
     cudaFree(h->d_my);
@@ -404,7 +466,6 @@ static int one_pair(esp_handle *h, int mode, const uint8_t *read, size_t m, cons
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
-    if (m > (size_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     CK(h, cudaSetDevice(h->device));
     std::vector<esp_n_interval> iv;
     uint64_t wpos = ((m + 63) / 64) * 64;  // window starts on a 16-byte boundary
@@ -588,7 +649,6 @@ int esp_batch_extend_host(esp_handle *h, int mode, const esp_pair *pairs, uint64
     ScanOut all;
     for (auto &s : sc) merge(all, s);
     const Limits &L1 = all.L1, &L2 = all.L2;
-    if (L1.max_m > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     size_t sz_pairs = (n_pairs * sizeof(esp_pair) + 255) / 256 * 256;
     size_t sz_iv = (n_iv_count * sizeof(esp_n_interval) + 255) / 256 * 256;
     size_t sz_arena = (arena_bytes + 16 + 255) / 256 * 256;
@@ -676,7 +736,6 @@ int esp_batch_extend_device(esp_handle *h, int mode, const esp_pair *pairs, uint
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
-    if (limits->max_read_len > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     CK(h, cudaSetDevice(h->device));
     Limits L1, L2;
     if (mode == ESP_MODE_HINT) {

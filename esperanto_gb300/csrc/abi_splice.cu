@@ -172,7 +172,6 @@ int esp_retry_tail_start(esp_handle *h, const esp_genome *g, const uint8_t *read
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
-    if (read_len > (size_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     CK(h, cudaSetDevice(h->device));
     // staging: read record | candidate | N intervals | read arena
     std::vector<esp_n_interval> iv;
@@ -257,7 +256,6 @@ int esp_batch_splice_host(esp_handle *h, const esp_genome *g, const esp_splice_r
             (uint64_t)R.n_first + R.n_read > read_n_iv_count)
             return fail(h, ESP_EINVAL, "read record outside its tables");
         maxL = std::max(maxL, R.read_len);
-        if (R.read_len > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     }
     CK(h, cudaSetDevice(h->device));
     size_t s_r = al256(n_reads * sizeof(esp_splice_read));
@@ -317,7 +315,6 @@ int esp_batch_splice_device(esp_handle *h, const esp_genome *g, const esp_splice
     esp::GotohConst K;
     if (esp::make_gotoh_const(*params, K) != ESP_OK)
         return fail(h, ESP_EDOMAIN, "scoring parameters outside the device domain");
-    if (max_read_len > (uint32_t)K.max_m) return fail(h, ESP_EDOMAIN, "read too long for the scoring parameters (scores must stay within the int16 row buffer: read length x largest substitution score <= 8191)");
     CK(h, cudaSetDevice(h->device));
     SpliceBufs B;
     cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;

@@ -21,22 +21,34 @@ static constexpr int NBINS = 1 << (2 * KEY_BITS);
 static constexpr int SCAN_TILE = 1024;  // counters per block of the scan
 static constexpr int SCAN_BLOCKS = NBINS / SCAN_TILE;
 
-// Key: larger = more expensive.  w = columns per row (band width or window),
-// m = rows.
+// Key: larger = more expensive.  m = rows; w = columns per row (band
+// width or window) in band mode and extend_hint's full-matrix attempt
+// (mode 2); in its banded first attempt (mode 1) the window length instead:
+// every first attempt has width 61 (or the window, up to 30), so the window
+// length orders them as well and, with the rows, pins their geometry
+// wherever the hint offset follows from the lengths (read + 2h windows at
+// offset h, flank segments at offset 0, fixed-shape reads).
 __device__ __forceinline__ uint32_t geometry_key(const esp_pair &P, int mode) {
     uint32_t m = P.read_len, n = P.win_len;
     uint32_t w;
-    bool full = (mode == 0) ? (P.band_half < 0) : (n <= 30);
-    if (full) {
+    bool full = (mode == 0) ? (P.band_half < 0) : (mode == 2 || n <= 30);
+    if (full || mode == 1) {
         w = n;
     } else {
-        uint32_t h = mode == 0 ? (uint32_t)P.band_half : 30u;
-        uint64_t bw = 2ull * h + 1;
+        uint64_t bw = 2ull * (uint32_t)P.band_half + 1;
         w = (uint32_t)(bw < n ? bw : n);
     }
     const uint32_t top = (1u << KEY_BITS) - 1;
     return ((w < top ? w : top) << KEY_BITS) | (m < top ? m : top);
 }
+
+// Entry k of the pairs to bin: k itself, or list[k] over *count entries.
+struct BinInput {
+    const uint32_t *list;   // null: pairs 0 .. n-1
+    const uint32_t *count;  // device count of list entries (list only)
+    __device__ __forceinline__ uint64_t size(uint64_t n) const { return list ? *count : n; }
+    __device__ __forceinline__ uint32_t at(uint64_t k) const { return list ? list[k] : (uint32_t)k; }
+};
 
 __device__ __forceinline__ void agg_add(uint32_t *ctr, uint32_t key, uint32_t *slot) {
     // warp-aggregated atomicAdd on ctr[key]; returns each lane's slot
@@ -51,11 +63,14 @@ __device__ __forceinline__ void agg_add(uint32_t *ctr, uint32_t key, uint32_t *s
     if (slot) *slot = base + rank;
 }
 
-__global__ void bin_hist(const esp_pair *__restrict__ pairs, uint64_t n, int mode,
+__global__ void bin_hist(const esp_pair *__restrict__ pairs, uint64_t n, BinInput in, int mode,
                          uint32_t *__restrict__ hist) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+    const uint64_t cnt = in.size(n);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t key = geometry_key(pairs[i], mode);
+        const uint32_t pi = in.at(i);
+        if (pi >= n) continue;  // never index past the batch
+        uint32_t key = geometry_key(pairs[pi], mode);
         agg_add(hist, NBINS - 1 - key, nullptr);  // descending cost order
     }
 }
@@ -142,14 +157,17 @@ __global__ void __launch_bounds__(256) bin_scan_down(uint32_t *__restrict__ hist
     tile[threadIdx.x] = r;
 }
 
-__global__ void bin_scatter(const esp_pair *__restrict__ pairs, uint64_t n, int mode,
+__global__ void bin_scatter(const esp_pair *__restrict__ pairs, uint64_t n, BinInput in, int mode,
                             uint32_t *__restrict__ cursor, uint32_t *__restrict__ order) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+    const uint64_t cnt = in.size(n);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t key = geometry_key(pairs[i], mode);
+        const uint32_t pi = in.at(i);
+        if (pi >= n) continue;
+        uint32_t key = geometry_key(pairs[pi], mode);
         uint32_t slot;
         agg_add(cursor, NBINS - 1 - key, &slot);
-        order[slot] = (uint32_t)i;
+        order[slot] = pi;
     }
 }
 
@@ -219,7 +237,9 @@ __global__ void class_bounds(const uint32_t *__restrict__ hist, const uint32_t *
 
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
                            uint32_t *order, int num_sms, cudaStream_t st, uint32_t *total,
-                           uint32_t *bounds, bool pad) {
+                           uint32_t *bounds, bool pad, const uint32_t *list,
+                           const uint32_t *list_count) {
+    const BinInput in{list, list_count};
     cudaError_t e = cudaMemsetAsync(hist, 0, bin_scratch_bytes(), st);
     if (e == cudaSuccess && pad)
         e = cudaMemsetAsync(order, 0xff, (n + bin_pad_slots(n)) * sizeof(uint32_t), st);
@@ -227,14 +247,14 @@ cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t
     int grid = num_sms * 4;
     uint64_t need = (n + 255) / 256;
     if ((uint64_t)grid > need) grid = (int)(need ? need : 1);
-    bin_hist<<<grid, 256, 0, st>>>(pairs, n, mode, hist);
+    bin_hist<<<grid, 256, 0, st>>>(pairs, n, in, mode, hist);
     if (pad) bin_scan_up<true><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
     else bin_scan_up<false><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
     bin_scan_top<<<1, 1024, 0, st>>>(hist + NBINS, total);
     if (pad) bin_scan_down<true><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
     else bin_scan_down<false><<<SCAN_BLOCKS, 256, 0, st>>>(hist, hist + NBINS);
     if (bounds) class_bounds<<<1, 32, 0, st>>>(hist, total, bounds);
-    bin_scatter<<<grid, 256, 0, st>>>(pairs, n, mode, hist, order);
+    bin_scatter<<<grid, 256, 0, st>>>(pairs, n, in, mode, hist, order);
     return cudaGetLastError();
 }
 

@@ -53,9 +53,12 @@ struct esp_handle {
     size_t d_rb_cap = 0;
     uint32_t *d_esc = nullptr;  // escalation list
     size_t d_esc_cap = 0;       // bytes
+    uint32_t *d_wide = nullptr; // pairs outside the int16 domain (the wide kernel's list)
+    size_t d_wide_cap = 0;      // bytes
     // d_ctr (256 B): u64 queues at [0..1] (attempt 1), [2..3] (attempt 2),
     // u32 esc count at [4], u64 class queues at [8..15], class bounds at
-    // [24..28], binned list length at [29]
+    // [24..28], binned list length at [29], wide-list count at [30], binned
+    // escalation list length at [31]
     uint32_t *d_ctr = nullptr;
     int tune[esp::kLengthClasses] = {-1, -1, -1, -1};  // DP variant per length class (autotuned)
     bool tuned = false;

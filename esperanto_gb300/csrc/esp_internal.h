@@ -54,6 +54,13 @@ struct GotohJob {
     uint32_t *rb;               // row-buffer scratch: slots * rb_words * 32 words
     uint64_t rb_words;
     uint32_t *queue;            // device work counter (zeroed before launch)
+    // Pairs outside the int16 domain (read longer than GotohConst::max_m):
+    // the int16 kernels append them to wide_list (count in *wide_count) and
+    // leave them to the wide kernel, which sets `wide` and runs them in
+    // int32; without a list they are refused per pair (ESP_EINVAL).
+    uint32_t *wide_list;
+    uint32_t *wide_count;
+    int wide;
 };
 
 // Launch the persistent DP kernel with `warps` warps total.
@@ -65,6 +72,15 @@ cudaError_t launch_gotoh(const GotohJob &job, const GotohConst &k, int warps, in
                          cudaStream_t st, int variant);
 constexpr int kGotohVariants = 4;
 constexpr bool gotoh_paired(int variant) { return variant >= 2; }
+
+// Wide DP kernel: one warp per pair of job.list (*job.list_count entries),
+// int32 scores, for pairs outside the int16 domain.  job.mode 0 runs each
+// pair's band (or full matrix); 1 runs the whole extend_hint policy (the
+// banded attempt, then the full matrix when it escalates).  Each warp owns
+// tb_words + 2 * rb_words words of job.tb (its row buffer holds H and E as
+// separate words).  Same results as the int16 kernels wherever both apply.
+cudaError_t launch_gotoh_wide(const GotohJob &job, const GotohConst &k, int warps,
+                              cudaStream_t st);
 
 // Warp-per-pair DP kernel (per-call drop-in, small batches): `warps` warps
 // stride over the pairs; each warp owns tb_words + rb_words words of the
@@ -143,9 +159,13 @@ cudaError_t launch_count_cells(const esp_pair *pairs, const esp_extension *out, 
 // bounds (optional, 5 device words): the four length classes of the list.
 // pad: every bin padded to an even slot count with NO_PAIR entries (order
 // needs n + bin_pad_slots(n) words), for the two-pairs-per-thread kernel.
+// mode: 0 band, 1 extend_hint's first attempt, 2 its full-matrix attempt.
+// list / list_count (device, optional): bin only the pairs list[0 ..
+// *list_count), n bounding the count (extend_hint's escalations).
 cudaError_t launch_binning(const esp_pair *pairs, uint64_t n, int mode, uint32_t *hist,
                            uint32_t *order, int num_sms, cudaStream_t st, uint32_t *total,
-                           uint32_t *bounds = nullptr, bool pad = false);
+                           uint32_t *bounds, bool pad, const uint32_t *list = nullptr,
+                           const uint32_t *list_count = nullptr);
 // Spare slots a padded list may add to n pairs (the list holds n + this).
 uint64_t bin_pad_slots(uint64_t n);
 constexpr int kLengthClasses = 4;

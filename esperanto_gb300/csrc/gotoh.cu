@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "esp_device.cuh"
 #include "esp_internal.h"
@@ -70,11 +71,17 @@ struct Seq {
     }
 };
 
-struct Strip {
-    int Hl[STRIP], Fl[STRIP], rk[STRIP];
+// Row-max keys are Hp * 32768 + (32767 - j): 32 bits while Hp < 65536 (the
+// int16 domain); the wide kernel keeps them in 64 bits.
+template <bool WIDE>
+struct StripT {
+    using RK = typename std::conditional<WIDE, long long, int>::type;
+    int Hl[STRIP], Fl[STRIP];
+    RK rk[STRIP];
     uint32_t l0[STRIP], l1[STRIP];
     int lo[STRIP], hi[STRIP];
 };
+using Strip = StripT<false>;
 
 __device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
     uint32_t d;  // integer multiply-add: issues on the FMA pipe, off the saturated ALU pipe
@@ -101,9 +108,10 @@ __device__ __forceinline__ uint32_t and_or_u32(uint32_t a, uint32_t m, uint32_t 
 // above at column j-1; cj = 32767 - j (row-max key tie order).  MASK = 1
 // tests every cell against its row window (strip ramps); MASK = 0 is the
 // strip interior where all 8 cells are in window.
-template <int MASK>
-__device__ __forceinline__ uint32_t dp_column(Strip &S, const GotohConst &K, int j, uint32_t sel,
-                                              uint32_t cj, int &upH, int &upE, int diag) {
+template <int MASK, bool WIDE = false>
+__device__ __forceinline__ uint32_t dp_column(StripT<WIDE> &S, const GotohConst &K, int j,
+                                              uint32_t sel, uint32_t cj, int &upH, int &upE,
+                                              int diag) {
     uint32_t wa = 0, wb = 0;
     int d = diag;
 #pragma unroll
@@ -122,7 +130,11 @@ __device__ __forceinline__ uint32_t dp_column(Strip &S, const GotohConst &K, int
         int Hp = (int)and_or_u32((uint32_t)key, ~3u, 2u);
         wa = mad_u32(wa, 4u, (uint32_t)(key - Hp + 2));
         wb = mad_u32(wb, 4u, (uint32_t)((kE - E4) + (kF - F4)));
-        int rkey = (int)mad_u32((uint32_t)Hp, 32768u, cj);
+        typename StripT<WIDE>::RK rkey;
+        if constexpr (WIDE)
+            rkey = ((long long)Hp << 15) | (long long)cj;
+        else
+            rkey = (int)mad_u32((uint32_t)Hp, 32768u, cj);
         if (MASK) {
             // An out-of-window cell shows H = 0, E = NEG to the row below and
             // leaves its row's state alone: before the window that is still
@@ -707,10 +719,15 @@ __device__ __forceinline__ bool setup_pair(const GotohJob &job, const GotohConst
     uint64_t need_rb = (uint64_t)sw;
     const uint8_t *warena = job.win_arena ? job.win_arena : job.arena;
     const uint64_t wbases = job.win_arena ? job.win_arena_bases : job.arena_bases;
-    if (need_tb > tb_cap || need_rb > rb_cap ||
-        (uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
-        P.read_pos + (uint64_t)m > job.arena_bases || P.win_pos + (uint64_t)n > wbases ||
-        m > 32767 || n > 32767 || m > K.max_m) {
+    const bool outside = (uint64_t)P.n_first + P.n_read + P.n_win > job.n_iv_count ||
+                         P.read_pos + (uint64_t)m > job.arena_bases ||
+                         P.win_pos + (uint64_t)n > wbases || m > 32767 || n > 32767;
+    if (!outside && m > K.max_m && !job.wide && job.wide_list) {
+        // scores may leave the int16 domain: the wide kernel runs this pair
+        if (write) job.wide_list[atomicAdd(job.wide_count, 1u)] = pi;
+        return false;
+    }
+    if (need_tb > tb_cap || need_rb > rb_cap || outside || (m > K.max_m && !job.wide)) {
         // scratch sized too small by the host, or the pair lies outside its
         // tables: refuse, never overrun
         o.status = ESP_EINVAL;
@@ -729,12 +746,14 @@ __device__ __forceinline__ bool setup_pair(const GotohJob &job, const GotohConst
 }
 
 // Traceback, CIGAR, TouchRec, extend_hint escalation (extend.rs:421-426),
-// then the result record.
+// then the result record.  Returns whether attempt 1 escalates; the pair is
+// appended to the escalation list when `queue` (the wide kernel runs its
+// second attempt itself).
 template <int TBS>
-__device__ __forceinline__ void finish_pair(const GotohJob &job, const GotohConst &K,
+__device__ __forceinline__ bool finish_pair(const GotohJob &job, const GotohConst &K,
                                             const int8_t *__restrict__ lut, uint32_t pi,
                                             PairSetup &S, const FillResult &F,
-                                            const uint32_t *tb) {
+                                            const uint32_t *tb, bool queue = true) {
     esp_extension &o = S.o;
     dp_finish<TBS>(K, lut, S.g, tb, S.sw, S.m, S.n, S.read, S.win, F, o, S.cig,
                    job.cigar_stride);
@@ -744,16 +763,18 @@ __device__ __forceinline__ void finish_pair(const GotohJob &job, const GotohCons
         o.touch_left = F.tleft ? 1 : 0;
         o.touch_clamped = F.tclamp ? 1 : 0;
     }
+    bool esc = false;
     if (job.mode == 1 && !S.full) {
         // escalate on a band-edge touch or < 85% of perfect
         int perfect = S.m * K.match;
         if (F.trow != 0 || o.score * 20 < perfect * 17) {
-            uint32_t slot = atomicAdd(job.esc_count, 1u);
-            job.esc_list[slot] = pi;
+            if (queue) job.esc_list[atomicAdd(job.esc_count, 1u)] = pi;
             o.escalated = 1;
+            esc = true;
         }
     }
     job.out[pi] = o;
+    return esc;
 }
 
 __device__ void process_pair(const GotohJob &job, const GotohConst &K,
@@ -814,6 +835,10 @@ __global__ void __launch_bounds__(128, MINB) gotoh_kernel(GotohJob job, GotohCon
 // (word stride 1).
 // ---------------------------------------------------------------------------
 
+// WIDE = false: H and E of a row cross lanes and passes packed as int16
+// halves of one word (the int16 domain); WIDE = true: as two int32 words
+// (the row buffer then holds 2 words per column).
+template <bool WIDE>
 __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict__ s_lut,
                                 const PairSetup &P, uint32_t *tb, uint32_t *rb, int lane) {
     const int m = P.m, n = P.n, sw = P.sw;
@@ -830,7 +855,7 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
         const bool act = s < nstrips;
         const int i0 = s * STRIP + 1;
         const int nact = act ? min(STRIP, m - i0 + 1) : 0;
-        Strip S;
+        StripT<WIDE> S;
 #pragma unroll
         for (int r = 0; r < STRIP; r++) {
             S.lo[r] = g.lo(i0 + r);
@@ -859,19 +884,34 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
         int t0 = act ? clo + lane : 0x7fffffff, t1 = act ? chi + lane : -1;
         t0 = __reduce_min_sync(0xffffffffu, t0);
         t1 = __reduce_max_sync(0xffffffffu, t1);
-        uint32_t pub = ABSENT;  // bottom row published at the end of a step
+        // bottom row published at the end of a step: packed (int16) or H / E (int32)
+        uint32_t pub = ABSENT;
+        int pubH = 2, pubE = NEG4;
         int diag = 2;           // H of the row above at the previous column
         if (lane == 0 && base && clo - 1 >= plo && clo - 1 <= phi)
-            diag = (int)(rb[clo - 1 - plo] & 0xffffu);
+            diag = WIDE ? (int)rb[2 * (clo - 1 - plo)] : (int)(rb[clo - 1 - plo] & 0xffffu);
         uint32_t *tbs = tb + (size_t)s * sw;
         const bool handoff = lane == 31 && s + 1 < nstrips;
         int cw_at = -1000000;  // first window position of the cached code word
         uint32_t cw = 0, cn = 0;
         for (int t = t0; t <= t1; t++) {
-            uint32_t in = __shfl_up_sync(0xffffffffu, pub, 1);
             const int j = t - lane;
-            if (lane == 0) in = (base && j >= plo && j <= phi) ? rb[j - plo] : ABSENT;
-            uint32_t out = ABSENT;
+            int inH, inE;
+            if (WIDE) {
+                inH = __shfl_up_sync(0xffffffffu, pubH, 1);
+                inE = __shfl_up_sync(0xffffffffu, pubE, 1);
+                if (lane == 0) {
+                    const bool have = base && j >= plo && j <= phi;
+                    inH = have ? (int)rb[2 * (j - plo)] : 2;
+                    inE = have ? (int)rb[2 * (j - plo) + 1] : NEG4;
+                }
+            } else {
+                uint32_t in = __shfl_up_sync(0xffffffffu, pub, 1);
+                if (lane == 0) in = (base && j >= plo && j <= phi) ? rb[j - plo] : ABSENT;
+                inH = (int)(in & 0xffffu);
+                inE = ((int)in) >> 16;
+            }
+            int outH = 2, outE = NEG4;
             if (act && j >= clo && j <= chi) {
                 // window codes 16 at a time (a load per column would sit on
                 // the wavefront's critical path)
@@ -883,14 +923,28 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
                 const int sh = j - 1 - cw_at;
                 uint32_t code = ((cn >> (31 - sh)) & 1u) ? 4u : ((cw >> (30 - 2 * sh)) & 3u);
                 uint32_t sel = code * 0x1111u + 0x8880u;
-                int upH = (int)(in & 0xffffu), upE = ((int)in) >> 16;
-                uint32_t word = dp_column<1>(S, K, j, sel, 32767u - (uint32_t)j, upH, upE, diag);
+                int upH = inH, upE = inE;
+                uint32_t word = dp_column<1, WIDE>(S, K, j, sel, 32767u - (uint32_t)j, upH, upE,
+                                                   diag);
                 tbs[j - clo] = word;
-                out = __byte_perm((uint32_t)upH, (uint32_t)upE, 0x5410);
-                if (handoff && j >= lo7) rb[j - lo7] = out;
+                outH = upH;
+                outE = upE;
+                if (handoff && j >= lo7) {
+                    if (WIDE) {
+                        rb[2 * (j - lo7)] = (uint32_t)upH;
+                        rb[2 * (j - lo7) + 1] = (uint32_t)upE;
+                    } else {
+                        rb[j - lo7] = __byte_perm((uint32_t)upH, (uint32_t)upE, 0x5410);
+                    }
+                }
             }
-            diag = (int)(in & 0xffffu);
-            pub = out;
+            diag = inH;
+            if (WIDE) {
+                pubH = outH;
+                pubE = outE;
+            } else {
+                pub = __byte_perm((uint32_t)outH, (uint32_t)outE, 0x5410);
+            }
         }
         __syncwarp();
         // this lane's rows, in row order (extend.rs:795-827)
@@ -899,8 +953,8 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
 #pragma unroll
         for (int r = 0; r < STRIP; r++) {
             if (r < nact) {
-                int rowHp = S.rk[r] >> 15;
-                int argj = 32767 - (S.rk[r] & 32767);
+                int rowHp = (int)(S.rk[r] >> 15);
+                int argj = 32767 - (int)(S.rk[r] & 32767);
                 if (trow == 0) {
                     if (argj == S.lo[r]) {
                         trow = i0 + r;
@@ -960,7 +1014,7 @@ __global__ void __launch_bounds__(128) gotoh_warp_kernel(GotohJob job, GotohCons
         const uint32_t pi = job.list ? job.list[k] : (uint32_t)k;
         PairSetup S;
         if (!setup_pair(job, K, pi, job.tb_words, job.rb_words, lane == 0, S)) continue;
-        FillResult F = warp_fill(K, s_lut, S, tb, rb, lane);
+        FillResult F = warp_fill<false>(K, s_lut, S, tb, rb, lane);
         __syncwarp();  // traceback words of every lane are visible to lane 0
         if (lane == 0) finish_pair<1>(job, K, s_lut25, pi, S, F, tb);
         __syncwarp();
@@ -971,6 +1025,58 @@ cudaError_t launch_gotoh_warp(const GotohJob &job, const GotohConst &k, int warp
                               cudaStream_t st) {
     int grid = (warps + 3) / 4;
     gotoh_warp_kernel<<<grid, 128, 0, st>>>(job, k);
+    return cudaGetLastError();
+}
+
+// Pairs outside the int16 domain (reads longer than GotohConst::max_m), one
+// warp per pair with int32 H / E / F and 64-bit row-max keys, otherwise the
+// warp-per-pair fill and the same traceback: the same cells, words, maxima,
+// touches and CIGARs as the reference's i32 flavour of run_band
+// (extend.rs:462-528).  In hint mode the warp runs extend_hint's second
+// attempt itself when the first escalates (extend.rs:421-426).
+__global__ void __launch_bounds__(128) gotoh_wide_kernel(GotohJob job, GotohConst K) {
+    __shared__ uint32_t s_lut[10];
+    __shared__ int8_t s_lut25[32];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) s_lut[k] = K.lut4[k >> 1][k & 1];
+#pragma unroll
+        for (int k = 0; k < 25; k++) s_lut25[k] = K.lut[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp_slot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t *tb = job.tb + warp_slot * (job.tb_words + 2 * job.rb_words);
+    uint32_t *rb = tb + job.tb_words;
+    const uint64_t total = *job.list_count;
+    for (uint64_t k = warp_slot; k < total; k += n_warps) {
+        const uint32_t pi = job.list[k];
+        PairSetup S;
+        if (!setup_pair(job, K, pi, job.tb_words, job.rb_words, lane == 0, S)) continue;
+        FillResult F = warp_fill<true>(K, s_lut, S, tb, rb, lane);
+        __syncwarp();
+        int esc = 0;
+        if (lane == 0) esc = finish_pair<1>(job, K, s_lut25, pi, S, F, tb, false) ? 1 : 0;
+        esc = __shfl_sync(0xffffffffu, esc, 0);
+        __syncwarp();
+        if (!esc) continue;
+        GotohJob j2 = job;
+        j2.mode = 2;
+        if (!setup_pair(j2, K, pi, job.tb_words, job.rb_words, lane == 0, S)) continue;
+        F = warp_fill<true>(K, s_lut, S, tb, rb, lane);
+        __syncwarp();
+        if (lane == 0) finish_pair<1>(j2, K, s_lut25, pi, S, F, tb, false);
+        __syncwarp();
+    }
+}
+
+cudaError_t launch_gotoh_wide(const GotohJob &job, const GotohConst &k, int warps,
+                              cudaStream_t st) {
+    GotohJob j = job;
+    j.wide = 1;
+    int grid = (warps + 3) / 4;
+    gotoh_wide_kernel<<<grid, 128, 0, st>>>(j, k);
     return cudaGetLastError();
 }
 

@@ -198,8 +198,8 @@ extern "C" int esp_batch_spliced_host(esp_handle *h, const esp_genome *g,
                 return fail(h, ESP_EINVAL, "exons overlap or are out of order");
             total += x.end - x.start;
         }
-        if (R.read_len > (uint32_t)K.max_m || total > 32767)
-            return fail(h, ESP_EDOMAIN, "read or pseudo-reference too long for the device DP");
+        if (R.read_len > 32767 || total > 32767)
+            return fail(h, ESP_EDOMAIN, "read or pseudo-reference longer than 32767");
         dev[r] = SplicedDev{pseudo_bases, R.exon_first, R.exon_count, R.contig, 0};
         esp_pair &P = pairs[r];
         P.read_pos = R.read_pos;

@@ -128,8 +128,10 @@ def lib():
         L.orc_run_dispatch.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), C.c_int, i64,
                                        i64, i64, i64, C.POINTER(_Ext), C.POINTER(_Touch)]
         L.orc_extend.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), C.POINTER(_Ext)]
-        L.orc_extend_hint.argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), i64, C.c_uint32,
-                                      C.c_uint32, C.POINTER(_Ext), C.POINTER(C.c_int)]
+        for name in ("orc_extend_hint", "orc_extend_hint_i32"):
+            getattr(L, name).argtypes = [u8p, i64, u8p, i64, C.POINTER(_Params), i64,
+                                         C.c_uint32, C.c_uint32, C.POINTER(_Ext),
+                                         C.POINTER(C.c_int)]
         L.orc_band_cells.argtypes = [i64, i64, C.c_int, i64, i64]
         L.orc_band_cells.restype = i64
         L.orc_i16_add.argtypes = [C.c_int16, C.c_int16]
@@ -282,15 +284,17 @@ def extend(read, win, params: Params = Params()) -> Ext:
 
 
 def extend_hint(read, win, params: Params = Params(), offset: int = 0,
-                with_escalation: bool = False):
+                with_escalation: bool = False, wide: bool = False):
+    """extend_hint (extend.rs:392-428); wide = every attempt in the i32
+    flavour of run_band (extend.rs:462-528)."""
     read, win = _b(read), _b(win)
     p = params.c()
     esc = C.c_int(0)
     cap = 2 * (len(read) + len(win)) + 8
     buf = (C.c_uint32 * cap)()
     e = _Ext(0, 0, 0, 0, 0, cap, buf)
-    rc = lib().orc_extend_hint(read, len(read), win, len(win), C.byref(p), offset, 1, 1,
-                               C.byref(e), C.byref(esc))
+    fn = lib().orc_extend_hint_i32 if wide else lib().orc_extend_hint
+    rc = fn(read, len(read), win, len(win), C.byref(p), offset, 1, 1, C.byref(e), C.byref(esc))
     if rc != 0:
         raise OracleError(f"orc_extend_hint returned {rc}")
     ext = Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops]))

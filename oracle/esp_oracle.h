@@ -88,6 +88,10 @@ int orc_extend(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
 int orc_extend_hint(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
                     const orc_params *p, int64_t offset, uint32_t num, uint32_t den,
                     orc_ext *out, int *escalated);
+/* extend_hint with every attempt in the i32 flavour of run_band. */
+int orc_extend_hint_i32(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
+                    const orc_params *p, int64_t offset, uint32_t num, uint32_t den,
+                    orc_ext *out, int *escalated);
 /* In-window cell count of one run_band call (the GCUPS work unit). */
 int64_t orc_band_cells(int64_t m, int64_t n, int has_band, int64_t offset, int64_t half);
 

@@ -477,22 +477,44 @@ int orc_extend(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
     return orc_run_dispatch(read, m, rf, n, p, 0, 0, 1, 1, 0, out, &t);
 }
 
-int orc_extend_hint(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
-                    const orc_params *p, int64_t offset, uint32_t num, uint32_t den,
-                    orc_ext *out, int *escalated) {
+/* extend.rs:392-428 extend_hint; with force_i32 every attempt runs the i32
+ * flavour of run_band (extend.rs:462-528) instead of run_dispatch's choice,
+ * which is what the wide device kernel reproduces for reads whose scores
+ * leave the i16 range. */
+static int extend_hint_impl(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
+                            const orc_params *p, int64_t offset, uint32_t num, uint32_t den,
+                            orc_ext *out, int *escalated, int force_i32) {
     if (escalated) *escalated = 0;
     if (m == 0 || n == 0) return empty_extension((uint32_t)m, out);
     orc_touch t;
-    if (INITIAL_BAND >= n) return orc_run_dispatch(read, m, rf, n, p, 0, 0, 1, 1, 0, out, &t);
-    int rc = orc_run_dispatch(read, m, rf, n, p, 1, offset, (int64_t)num,
-                              (int64_t)(den > 1 ? den : 1), INITIAL_BAND, out, &t);
+    if (INITIAL_BAND >= n)
+        return force_i32 ? orc_run_band(read, m, rf, n, p, 1, 0, 0, 1, 1, 0, out, &t)
+                         : orc_run_dispatch(read, m, rf, n, p, 0, 0, 1, 1, 0, out, &t);
+    int rc = force_i32
+                 ? orc_run_band(read, m, rf, n, p, 1, 1, offset, (int64_t)num,
+                                (int64_t)(den > 1 ? den : 1), INITIAL_BAND, out, &t)
+                 : orc_run_dispatch(read, m, rf, n, p, 1, offset, (int64_t)num,
+                                    (int64_t)(den > 1 ? den : 1), INITIAL_BAND, out, &t);
     if (rc != ORC_OK && rc != ORC_ECAP) return rc;
     int32_t perfect = (int32_t)m * p->match_score;
     if (t.touched || out->score * 20 < perfect * 17) {
         if (escalated) *escalated = 1;
-        return orc_run_dispatch(read, m, rf, n, p, 0, 0, 1, 1, 0, out, &t);
+        return force_i32 ? orc_run_band(read, m, rf, n, p, 1, 0, 0, 1, 1, 0, out, &t)
+                         : orc_run_dispatch(read, m, rf, n, p, 0, 0, 1, 1, 0, out, &t);
     }
     return rc;
+}
+
+int orc_extend_hint(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
+                    const orc_params *p, int64_t offset, uint32_t num, uint32_t den,
+                    orc_ext *out, int *escalated) {
+    return extend_hint_impl(read, m, rf, n, p, offset, num, den, out, escalated, 0);
+}
+
+int orc_extend_hint_i32(const uint8_t *read, int64_t m, const uint8_t *rf, int64_t n,
+                        const orc_params *p, int64_t offset, uint32_t num, uint32_t den,
+                        orc_ext *out, int *escalated) {
+    return extend_hint_impl(read, m, rf, n, p, offset, num, den, out, escalated, 1);
 }
 
 /* Cells in the windows of rows 1..m under the band rules of :653-696. */

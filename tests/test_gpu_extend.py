@@ -15,7 +15,7 @@ if not torch.cuda.is_available():
 
 import esperanto_gb300 as E  # noqa: E402
 from esperanto_gb300 import batch as B  # noqa: E402
-from gpu_helpers import _compare, compare, kernel_buffer  # noqa: E402
+from gpu_helpers import _compare, compare, gpu_batch, kernel_buffer  # noqa: E402
 import workloads as W  # noqa: E402
 
 
@@ -164,20 +164,68 @@ def test_cigar_capacity_reported():
         buf.check(rc)
 
 
-def test_score_range_domain():
-    """The row buffer holds H and E in int16 lanes: reads up to 8191 / (largest
-    substitution score) bases run (4095 at the default +2 match) and match the
-    oracle; one base more is refused with ESP_EDOMAIN instead of wrapping."""
+def _long_pair(rng, m, n, indels=True):
+    """A read of m bases planted in a window of n with substitutions and,
+    when asked, a few short indels."""
+    win = rng.choice(list("ACGT"), n)
+    s = int(rng.integers(0, max(1, n - m)))
+    read = list(win[s:s + m]) + list(rng.choice(list("ACGT"), max(0, m - (n - s))))
+    for q in rng.choice(m, m // 200 + 1, replace=False):
+        read[int(q)] = str(rng.choice(list("ACGT")))
+    if indels:
+        for q in sorted(rng.choice(np.arange(10, m - 10), 4, replace=False), reverse=True):
+            if rng.random() < 0.5:
+                read.pop(int(q))
+                read.append("A")
+            else:
+                read.insert(int(q), "C")
+                read.pop()
+    return "".join(read[:m]).encode(), "".join(win).encode(), s
+
+
+def test_wide_reads_match_the_i32_flavour():
+    """Reads whose scores leave the int16 row buffer (longer than 8191 /
+    largest substitution score: 4,095 bases at the default +2 match) run in
+    the int32 wide kernel instead of being refused, and return what the
+    reference's i32 flavour of run_band returns (extend.rs:462-528), up to
+    20,000-base reads with scores above 32,767: per call and in batches
+    mixed with int16-domain pairs, band and full matrix, every EditDir."""
     rng = np.random.default_rng(77)
-    read = "".join(rng.choice(list("ACGT"), 4095))
-    win = "AC" + read[:2000] + "G" + read[2000:] + "TT"
-    got, _ = E.run_band(read, win, band=(2, 40))
-    want, _ = O.run_dispatch(read, win, band=(2, 40))
-    assert got.score == want.score and got.key() == want.key()
-    assert got.score > 8000
-    with pytest.raises(E.EspError) as ei:
-        E.run_band(read + "A", win + "A", band=(2, 40))
-    assert ei.value.code == -4  # ESP_EDOMAIN
+    cases = []  # (read, win, band or None, edit_dir)
+    for m, n, band in ((4095, 4200, (2, 40)), (4096, 4200, (2, 40)), (5000, 5100, None),
+                       (8191, 8300, (30, 64)), (12000, 12100, (40, 30)),
+                       (20000, 20000, (0, 30)), (20000, 20050, (10, 128)), (6000, 6000, None)):
+        read, win, s = _long_pair(rng, m, n)
+        off = band[0] if band else 0
+        cases.append((read, win, (s + off, band[1]) if band else None, len(cases) % 3))
+    for read, win, band, d in cases:
+        want, wt = O.run_band(read, win, O.Params(edit_dir=d), wide=True, band=band)
+        got, gt = E.run_band(read, win, E.ExtendParams(edit_dir=d), band=band)
+        assert got.key() == want.key(), (len(read), band, d)
+        assert (gt.touched, gt.row, gt.left) == (wt.touched, wt.row, wt.left)
+    assert max(O.run_band(c[0], c[1], wide=True, band=c[2])[0].score for c in cases) > 32767
+    # extend_hint on long reads (both attempts in the wide kernel)
+    for read, win, band, d in cases[:5]:
+        want = O.extend_hint(read, win, O.Params(edit_dir=d), offset=band[0] if band else 0)
+        got = E.extend_hint(read, win, E.ExtendParams(edit_dir=d),
+                            hint=E.DiagHint(band[0] if band else 0))
+        assert got.key() == want.key(), (len(read), d)
+    # batches: long pairs among 150 x 214 pairs, on every DP kernel, band and hint
+    short = []
+    for k in range(300):
+        read, win, s = _long_pair(rng, 150, 214, indels=k % 2 == 0)
+        short.append((read, win, (s, 32)))
+    mixed = short[:150] + [(c[0], c[1], c[2]) for c in cases[:6]] + short[150:]
+    for kern in ("warp", "thread", "paired"):
+        for mode in (B.MODE_BAND, B.MODE_HINT):
+            got = gpu_batch(mixed, 0, mode, cigar_stride=64, kernel=kern)
+            for k, (read, win, band) in enumerate(mixed):
+                if mode == B.MODE_BAND:
+                    want = O.run_band(read, win, O.Params(), wide=True, band=band)[0].key()
+                else:
+                    want = O.extend_hint(read, win, O.Params(),
+                                         offset=band[0] if band else 0).key()
+                assert got[k][0] == want, (kern, mode, k, len(read))
 
 
 def test_graph_replay_of_identical_device_batches():
