@@ -205,6 +205,20 @@ def lib():
     L.esp_server_wait.argtypes = [vp, C.c_uint64, C.c_int, C.POINTER(C.c_int32),
                                   C.POINTER(C.c_double)]
     L.esp_server_get_stats.argtypes = [vp, C.POINTER(ServerStatsC)]
+    L.esp_chunk_create.argtypes = [vp, C.c_uint32, C.POINTER(vp)]
+    L.esp_chunk_add_extend_hint.argtypes = [vp, u8p, sz, u8p, sz, C.c_int64,
+                                            C.POINTER(C.c_uint64)]
+    L.esp_chunk_add_run_band.argtypes = [vp, u8p, sz, u8p, sz, C.c_int64, C.c_int64,
+                                         C.POINTER(C.c_uint64)]
+    L.esp_chunk_add_extend.argtypes = [vp, u8p, sz, u8p, sz, C.POINTER(C.c_uint64)]
+    L.esp_chunk_add_myers.argtypes = [vp, C.c_int, u8p, sz, u8p, sz, C.POINTER(C.c_uint64)]
+    L.esp_chunk_run.argtypes = [vp, C.POINTER(ExtendParamsC)]
+    L.esp_chunk_extension.argtypes = [vp, C.c_uint64, C.POINTER(ExtensionC), vp, C.c_uint32]
+    L.esp_chunk_myers.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]
+    L.esp_chunk_size.argtypes = [vp]
+    L.esp_chunk_size.restype = C.c_uint64
+    L.esp_chunk_reset.argtypes = [vp]
+    L.esp_chunk_destroy.argtypes = [vp]
     L.esp_server_close.argtypes = [vp]
     L.esp_server_destroy.argtypes = [vp]
     L.esp_last_cells.argtypes = [vp]

@@ -581,6 +581,62 @@ int esp_server_get_stats(esp_server *s, esp_server_stats *out);
 int esp_server_close(esp_server *s);
 int esp_server_destroy(esp_server *s);
 
+/* ---- pipeline batching hook: a chunk collector over the batch API ----
+ *
+ * The reference's mapper aligns chunks of 100,000 reads, its rayon workers
+ * calling the per-read entry points one read at a time
+ * (crates/map/src/pipeline.rs:394-403 in run_pe, :116-250 run_se,
+ * :318-450).  A collector instead gathers a chunk's calls -- from any number
+ * of host threads at once; the add functions are thread-safe -- and
+ * esp_chunk_run sends each kind through the batch API as one batch (one per
+ * DP mode, one per Myers direction).  Each add returns the request's index
+ * (input order); after the run, esp_chunk_extension / esp_chunk_myers return
+ * exactly what the per-call entry point returns for it (the same guards:
+ * empty reads, Myers lengths, CIGAR capacity).  A pipeline whose per-read
+ * decisions depend on earlier results (Myers first, the DP only for reads
+ * Myers does not settle) runs rounds: add, run, read, reset.  ASCII inputs
+ * are copied at add time. */
+typedef struct esp_chunk esp_chunk;
+
+/* Kinds of esp_chunk_add_myers: myers_ea::{infix, infix_best_end,
+ * infix_best_start} (myers_ea.rs:118-185), their long:: forms (:249-310),
+ * esperanto_engine::myers::{infix, global} (engine/src/myers.rs:32-63). */
+#define ESP_CHUNK_MYERS_INFIX 0
+#define ESP_CHUNK_MYERS_BEST_END 1
+#define ESP_CHUNK_MYERS_BEST_START 2
+#define ESP_CHUNK_MYERS_LONG_INFIX 3
+#define ESP_CHUNK_MYERS_LONG_BEST_END 4
+#define ESP_CHUNK_MYERS_LONG_BEST_START 5
+#define ESP_CHUNK_ENGINE_INFIX 6
+#define ESP_CHUNK_ENGINE_GLOBAL 7
+
+/* A collector running its batches on handle h (one collector per handle);
+ * DP results keep cigar_stride ops per request (longer CIGARs report
+ * ESP_ECAP, as the per-call entry point with that capacity does). */
+int esp_chunk_create(esp_handle *h, uint32_t cigar_stride, esp_chunk **out);
+/* extend_hint (extend.rs:392-428), run_band (:606-851), extend (:347-354). */
+int esp_chunk_add_extend_hint(esp_chunk *c, const uint8_t *read, size_t read_len,
+                              const uint8_t *ref_window, size_t window_len, int64_t hint_offset,
+                              uint64_t *index);
+int esp_chunk_add_run_band(esp_chunk *c, const uint8_t *read, size_t read_len,
+                           const uint8_t *ref_window, size_t window_len, int64_t band_offset,
+                           int64_t band_half, uint64_t *index);
+int esp_chunk_add_extend(esp_chunk *c, const uint8_t *read, size_t read_len,
+                         const uint8_t *ref_window, size_t window_len, uint64_t *index);
+int esp_chunk_add_myers(esp_chunk *c, int kind, const uint8_t *read, size_t read_len,
+                        const uint8_t *text, size_t text_len, uint64_t *index);
+/* Run everything queued (one batch per kind, synchronously).  ESP_EBUSY if
+ * already run since the last reset. */
+int esp_chunk_run(esp_chunk *c, const esp_extend_params *params);
+/* Results by request index, as the per-call entry points return them. */
+int esp_chunk_extension(esp_chunk *c, uint64_t index, esp_extension *out, uint32_t *cigar,
+                        uint32_t cigar_cap);
+int esp_chunk_myers(esp_chunk *c, uint64_t index, int32_t *dist, uint64_t *pos);
+uint64_t esp_chunk_size(esp_chunk *c);
+/* Forget the queued requests and results (capacity is kept). */
+int esp_chunk_reset(esp_chunk *c);
+int esp_chunk_destroy(esp_chunk *c);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----
  *
  * esp_batch_run_band_noalloc: the same banded/full-matrix DP with traceback
