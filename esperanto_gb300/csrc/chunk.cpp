@@ -61,6 +61,7 @@ struct Batch {
 // Where request i's answer is: a record of a batch, or settled at add time.
 struct Entry {
     int8_t klass = -1;  // -1: immediate Myers answer
+    bool dist_only = false;  // a Myers kind that returns a distance alone
     uint64_t rec = 0;
     int32_t dist = 0;
     uint64_t pos = 0;
@@ -123,6 +124,8 @@ int add_myers(esp_chunk *c, int kind, const uint8_t *read, size_t m, const uint8
     if (n > 0xffffffffull) return ESP_EDOMAIN;
     int klass;
     bool single = false, engine = false;
+    const bool dist_only = kind == ESP_CHUNK_MYERS_INFIX || kind == ESP_CHUNK_MYERS_LONG_INFIX ||
+                           kind == ESP_CHUNK_ENGINE_INFIX || kind == ESP_CHUNK_ENGINE_GLOBAL;
     switch (kind) {
     case ESP_CHUNK_MYERS_INFIX: single = true; klass = K_MY_END; break;
     case ESP_CHUNK_MYERS_BEST_END: single = true; klass = K_MY_END; break;
@@ -143,6 +146,7 @@ int add_myers(esp_chunk *c, int kind, const uint8_t *read, size_t m, const uint8
     std::lock_guard<std::mutex> lk(c->mu);
     if (c->ran) return ESP_EBUSY;
     Entry e;
+    e.dist_only = dist_only;
     if (!engine && (m == 0 || m > (size_t)LONG_MAX_M)) {  // answered without a DP
         e.dist = (int32_t)(m == 0 ? 0 : m);
         *index = c->entries.size();
@@ -282,7 +286,7 @@ int esp_chunk_myers(esp_chunk *c, uint64_t index, int32_t *dist, uint64_t *pos) 
     const esp_myers_result &r = c->b[e.klass].mout[e.rec];
     if (r.status != ESP_OK) return fail(c->h, r.status, "myers kernel refused the pair");
     if (dist) *dist = r.dist;
-    if (pos) *pos = r.pos;
+    if (pos) *pos = e.dist_only ? 0 : r.pos;
     return ESP_OK;
 }
 

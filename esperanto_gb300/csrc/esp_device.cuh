@@ -64,6 +64,77 @@ __device__ __forceinline__ uint32_t code5(const uint8_t *__restrict__ arena, uin
     return load1(arena, pos + (uint64_t)q);
 }
 
+// A resident genome as kernels see it: the 2-bit arena and the merged N
+// intervals of every contig (contig C owns iv[C.n_first, C.n_first + C.n_count)).
+struct GenomeView {
+    const uint8_t *arena;
+    const esp_n_interval *iv;
+};
+
+// fasta.rs:117-134: binary search over the contig's merged N intervals.
+__device__ __forceinline__ bool genome_is_n(const GenomeView &G, const esp_contig &C,
+                                            uint32_t pos) {
+    uint32_t lo = 0, hi = C.n_count;
+    const esp_n_interval *iv = G.iv + C.n_first;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (pos < iv[mid].start) hi = mid;
+        else if (pos >= iv[mid].end) lo = mid + 1;
+        else return true;
+    }
+    return false;
+}
+
+// Base code (0..3, 4 = N) of contig position pos (fasta.rs:105-116 base).
+__device__ __forceinline__ uint32_t genome_code(const GenomeView &G, const esp_contig &C,
+                                                uint32_t pos) {
+    return genome_is_n(G, C, pos) ? 4u : load1(G.arena, C.base + pos);
+}
+
+// ASCII base of contig position pos (base + to_ascii).
+__device__ __forceinline__ uint8_t genome_ascii(const GenomeView &G, const esp_contig &C,
+                                                uint32_t pos) {
+    const uint8_t B[5] = {'A', 'C', 'G', 'T', 'N'};
+    return B[genome_code(G, C, pos)];
+}
+
+// splice.rs:324-340 dinuc (donor at p, acceptor ending at p; N-padded)
+__device__ __forceinline__ void genome_dinuc(const GenomeView &G, const esp_contig &C, uint32_t p,
+                                             bool donor, uint8_t out[2]) {
+    out[0] = out[1] = 'N';
+    if (!donor && p < 2) return;
+    uint32_t a = donor ? p : p - 2, b = donor ? p + 2 : p;
+    if (a >= C.len) return;
+    if (b > C.len) b = C.len;
+    for (uint32_t q = a; q < b; q++) out[q - a] = genome_ascii(G, C, q);
+}
+
+// splice.rs:78-103 splice_signal (inputs are uppercase here)
+__device__ __forceinline__ int splice_signal_of(const uint8_t d[2], const uint8_t a[2],
+                                                bool minus) {
+    auto is = [](const uint8_t x[2], char c0, char c1) { return x[0] == c0 && x[1] == c1; };
+    if (!minus) {
+        if (is(d, 'G', 'T') && is(a, 'A', 'G')) return ESP_SIG_GTAG;
+        if (is(d, 'G', 'C') && is(a, 'A', 'G')) return ESP_SIG_GCAG;
+        if (is(d, 'A', 'T') && is(a, 'A', 'C')) return ESP_SIG_ATAC;
+        return ESP_SIG_NONCANONICAL;
+    }
+    if (is(d, 'C', 'T') && is(a, 'A', 'C')) return ESP_SIG_GTAG;
+    if (is(d, 'C', 'T') && is(a, 'G', 'C')) return ESP_SIG_GCAG;
+    if (is(d, 'G', 'T') && is(a, 'A', 'T')) return ESP_SIG_ATAC;
+    return ESP_SIG_NONCANONICAL;
+}
+
+// splice.rs:63-71 SpliceSignal::score
+__device__ __forceinline__ int signal_bonus(int sig, const esp_splice_params &sp) {
+    switch (sig) {
+    case ESP_SIG_GTAG: return sp.gt_ag_bonus;
+    case ESP_SIG_GCAG: return sp.gc_ag_bonus;
+    case ESP_SIG_ATAC: return sp.at_ac_bonus;
+    default: return -sp.noncanonical_penalty;
+    }
+}
+
 // PTX prmt in its default mode: selector nibble bit 3 replicates the sign of
 // the selected byte, so a selector of c*0x1111 + 0x8880 returns byte c of
 // {hi:lo} sign-extended to 32 bits.

@@ -31,58 +31,25 @@ constexpr int SPL_MARGIN = 30; // split.rs:60 TAIL_MARGIN
 constexpr int SPL_COST = 4;    // splice.rs:57 SPLIT_COST
 
 __device__ __forceinline__ bool g_is_n(const SpliceJob &J, const esp_contig &C, uint32_t pos) {
-    // fasta.rs:117-134 binary search over the contig's merged N intervals
-    uint32_t lo = 0, hi = C.n_count;
-    const esp_n_interval *iv = J.g_iv + C.n_first;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (pos < iv[mid].start) hi = mid;
-        else if (pos >= iv[mid].end) lo = mid + 1;
-        else return true;
-    }
-    return false;
+    return genome_is_n(GenomeView{J.g_arena, J.g_iv}, C, pos);
 }
 
-// ASCII base of contig position pos (fasta.rs:105-116 base + to_ascii).
 __device__ __forceinline__ uint8_t g_base(const SpliceJob &J, const esp_contig &C, uint32_t pos) {
-    if (g_is_n(J, C, pos)) return 'N';
-    const uint8_t B[4] = {'A', 'C', 'G', 'T'};
-    return B[load1(J.g_arena, C.base + pos)];
+    return genome_ascii(GenomeView{J.g_arena, J.g_iv}, C, pos);
 }
 
-// splice.rs:324-340 dinuc (donor at p, acceptor ending at p; N-padded)
-__device__ void g_dinuc(const SpliceJob &J, const esp_contig &C, uint32_t p, bool donor,
-                        uint8_t out[2]) {
-    out[0] = out[1] = 'N';
-    if (!donor && p < 2) return;
-    uint32_t a = donor ? p : p - 2, b = donor ? p + 2 : p;
-    if (a >= C.len) return;
-    if (b > C.len) b = C.len;
-    for (uint32_t q = a; q < b; q++) out[q - a] = g_base(J, C, q);
+__device__ __forceinline__ void g_dinuc(const SpliceJob &J, const esp_contig &C, uint32_t p,
+                                        bool donor, uint8_t out[2]) {
+    genome_dinuc(GenomeView{J.g_arena, J.g_iv}, C, p, donor, out);
 }
 
-// splice.rs:78-103 splice_signal (inputs are uppercase here)
-__device__ int splice_signal_dev(const uint8_t d[2], const uint8_t a[2], bool minus) {
-    auto is = [](const uint8_t x[2], char c0, char c1) { return x[0] == c0 && x[1] == c1; };
-    if (!minus) {
-        if (is(d, 'G', 'T') && is(a, 'A', 'G')) return ESP_SIG_GTAG;
-        if (is(d, 'G', 'C') && is(a, 'A', 'G')) return ESP_SIG_GCAG;
-        if (is(d, 'A', 'T') && is(a, 'A', 'C')) return ESP_SIG_ATAC;
-        return ESP_SIG_NONCANONICAL;
-    }
-    if (is(d, 'C', 'T') && is(a, 'A', 'C')) return ESP_SIG_GTAG;
-    if (is(d, 'C', 'T') && is(a, 'G', 'C')) return ESP_SIG_GCAG;
-    if (is(d, 'G', 'T') && is(a, 'A', 'T')) return ESP_SIG_ATAC;
-    return ESP_SIG_NONCANONICAL;
+__device__ __forceinline__ int splice_signal_dev(const uint8_t d[2], const uint8_t a[2],
+                                                 bool minus) {
+    return splice_signal_of(d, a, minus);
 }
 
 __device__ __forceinline__ int signal_score_dev(int sig, const esp_splice_params &sp) {
-    switch (sig) {  // splice.rs:63-71
-    case ESP_SIG_GTAG: return sp.gt_ag_bonus;
-    case ESP_SIG_GCAG: return sp.gc_ag_bonus;
-    case ESP_SIG_ATAC: return sp.at_ac_bonus;
-    default: return -sp.noncanonical_penalty;
-    }
+    return signal_bonus(sig, sp);
 }
 
 struct Windows {

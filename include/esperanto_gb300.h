@@ -631,6 +631,7 @@ int esp_chunk_run(esp_chunk *c, const esp_extend_params *params);
 /* Results by request index, as the per-call entry points return them. */
 int esp_chunk_extension(esp_chunk *c, uint64_t index, esp_extension *out, uint32_t *cigar,
                         uint32_t cigar_cap);
+/* pos: the best end / best start of the kinds that return one, else 0. */
 int esp_chunk_myers(esp_chunk *c, uint64_t index, int32_t *dist, uint64_t *pos);
 uint64_t esp_chunk_size(esp_chunk *c);
 /* Forget the queued requests and results (capacity is kept). */

@@ -22,7 +22,7 @@ from typing import List, Optional, Sequence, Tuple
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libesp_oracle.so")
-SOURCES = ["extend.c", "myers.c", "split.c", "batch.c", "rescore.c", "spliced.c"]
+SOURCES = ["extend.c", "myers.c", "split.c", "batch.c", "rescore.c", "spliced.c", "intron.c"]
 
 OP_M, OP_I, OP_D, OP_N, OP_S = 0, 1, 2, 3, 4
 OP_CHARS = "MIDNS"
@@ -684,3 +684,86 @@ def align_spliced_exons(contig: "Contig", read, exons, params: Params = Params()
         raise OracleError(f"orc_align_spliced_exons returned {rc}")
     ext = Ext(e.read_start, e.read_end, e.ref_start, e.score, decode_ops(buf[:e.n_ops]))
     return ext, list(st[:ns.value]), gs.value
+
+
+# ---- intron-chain fast path (intron_chain.rs:285-538) ----
+
+class _LibEntry(C.Structure):
+    _fields_ = [("contig", C.c_uint32), ("start", C.c_uint32), ("end", C.c_uint32),
+                ("minus", C.c_int32), ("count", C.c_uint32)]
+
+
+class _Frag(C.Structure):
+    _fields_ = [("q_lo", C.c_uint32), ("q_hi", C.c_uint32), ("r_lo", C.c_uint32),
+                ("r_hi", C.c_uint32), ("n_anchors", C.c_uint32)]
+
+
+class _IntronParams(C.Structure):
+    _fields_ = [("min_frag_cov", C.c_uint32), ("refine_window", C.c_uint32),
+                ("refine_pattern_len", C.c_uint32), ("intron_max", C.c_uint32)]
+
+
+class _IntronOut(C.Structure):
+    _fields_ = [("found", C.c_int32), ("stage", C.c_int32), ("donor_end", C.c_uint32),
+                ("acceptor_start", C.c_uint32), ("vd", C.c_int32), ("va", C.c_int32),
+                ("junction", _Junction), ("signal", C.c_int32), ("support", C.c_uint32),
+                ("left_start", C.c_uint32), ("right_end", C.c_uint32), ("ext", _Ext),
+                ("stitched", C.POINTER(C.c_uint32)), ("stitched_cap", C.c_uint32),
+                ("n_stitched", C.c_uint32)]
+
+
+IC_STAGES = ("found", "empty", "anchors", "intron", "verify", "junction", "bounds", "result")
+
+
+@dataclass
+class IntronChain:
+    found: bool
+    stage: str
+    donor_end: int
+    acceptor_start: int
+    vd: int
+    va: int
+    junction: Tuple[int, int, bool]
+    signal: int
+    support: int
+    left_start: int
+    right_end: int
+    ext: Optional[Ext]
+    cigar: List[Tuple[str, int]]
+
+
+def intron_chain(contig: "Contig", contig_id: int, read, left, right, intron_start: int,
+                 intron_end: int, minus: bool, junction_lib=(), params: Params = Params(),
+                 refine_window: int = 30, refine_pattern_len: int = 50,
+                 intron_max: int = 105_000) -> IntronChain:
+    """try_intron_chain_placement (intron_chain.rs:392-538) from the best
+    fragment pair on.  left / right: (q_lo, q_hi, r_lo, r_hi, n_anchors);
+    junction_lib: (contig, start, end, minus, count) sorted as JunctionLib."""
+    r = _b(read)
+    jl = (_LibEntry * max(1, len(junction_lib)))(*[_LibEntry(*e) for e in junction_lib])
+    ip = _IntronParams(15, refine_window, refine_pattern_len, intron_max)
+    cap = 4 * len(r) + 64
+    eops = (C.c_uint32 * cap)()
+    sops = (C.c_uint32 * cap)()
+    o = _IntronOut()
+    o.ext.ops = eops
+    o.ext.cap = cap
+    o.stitched = sops
+    o.stitched_cap = cap
+    fn = lib().orc_intron_chain
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.c_char_p, C.c_uint32, C.POINTER(_Frag),
+                  C.POINTER(_Frag), C.c_uint32, C.c_uint32, C.c_int, C.c_void_p, C.c_uint64,
+                  C.POINTER(_IntronParams), C.POINTER(_Params), C.POINTER(_IntronOut)]
+    rc = fn(C.byref(contig.c), contig_id, r, len(r), C.byref(_Frag(*left)),
+            C.byref(_Frag(*right)), intron_start, intron_end, int(minus), C.cast(jl, C.c_void_p),
+            len(junction_lib), C.byref(ip), C.byref(params.c()), C.byref(o))
+    if rc != 0:
+        raise OracleError(f"orc_intron_chain returned {rc}")
+    ext = None
+    if o.stage in (0, 7):
+        ext = Ext(o.ext.read_start, o.ext.read_end, o.ext.ref_start, o.ext.score,
+                  decode_ops(eops[:o.ext.n_ops]))
+    return IntronChain(bool(o.found), IC_STAGES[o.stage], o.donor_end, o.acceptor_start, o.vd,
+                       o.va, (o.junction.start, o.junction.end, bool(o.junction.minus_strand)),
+                       o.signal, o.support, o.left_start, o.right_end, ext,
+                       decode_ops(sops[:o.n_stitched]) if o.stage in (0, 7) else [])

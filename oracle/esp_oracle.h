@@ -174,6 +174,58 @@ int orc_channel_a(const orc_contig *c, const uint8_t *read, uint32_t read_len,
                   const uint32_t *support, uint32_t n_cands, const orc_splice_params *sp,
                   const orc_params *p, orc_rescue *out);
 
+/* ---- intron-chain fast path, crates/map/src/intron_chain.rs ---- */
+typedef struct {  /* gtf.rs:72-149 JunctionLib entry, sorted (contig, start, end, minus) */
+    uint32_t contig, start, end;
+    int32_t minus;
+    uint32_t count;
+} orc_lib_entry;
+typedef struct {  /* intron_chain.rs:69-86 Frag (spans and anchor count) */
+    uint32_t q_lo, q_hi, r_lo, r_hi, n_anchors;
+} orc_frag;
+typedef struct {  /* intron_chain.rs:21-41 IntronParams */
+    uint32_t min_frag_cov, refine_window, refine_pattern_len, intron_max;
+} orc_intron_params;
+enum {  /* the stage that ended a read */
+    ORC_IC_FOUND = 0, ORC_IC_EMPTY = 1, ORC_IC_ANCHORS = 2, ORC_IC_INTRON = 3, ORC_IC_VERIFY = 4,
+    ORC_IC_JUNCTION = 5, ORC_IC_BOUNDS = 6, ORC_IC_RESULT = 7
+};
+typedef struct {
+    int32_t found, stage;
+    uint32_t donor_end, acceptor_start;
+    int32_t vd, va;
+    orc_junction junction;
+    int32_t signal;
+    uint32_t support;
+    uint32_t left_start, right_end;
+    orc_ext ext;              /* against the pseudo-reference (ops: caller buffer) */
+    uint32_t *stitched;       /* caller buffer */
+    uint32_t stitched_cap, n_stitched;
+} orc_intron_out;
+uint32_t orc_refine_donor_end(const orc_contig *c, const uint8_t *read, uint32_t len,
+                              uint32_t junction_off, uint32_t frag_ref_hi,
+                              int64_t frag_implied_start, uint32_t refine_window,
+                              uint32_t pattern_len);
+uint32_t orc_refine_acceptor_start(const orc_contig *c, const uint8_t *read, uint32_t len,
+                                   uint32_t junction_off, uint32_t frag_ref_lo,
+                                   int64_t frag_implied_start, uint32_t refine_window,
+                                   uint32_t pattern_len);
+void orc_verify_split_read(const orc_contig *c, const uint8_t *read, uint32_t len,
+                           int64_t left_off_lo, uint32_t right_r_hi, int64_t donor_end,
+                           int64_t acceptor_start, int32_t *vd, int32_t *va);
+uint32_t orc_lib_support(const orc_lib_entry *lib, uint64_t n, uint32_t contig, uint32_t start,
+                         uint32_t end, int minus);
+int orc_refine_junction_read(const orc_contig *c, uint32_t contig_id, const uint8_t *read,
+                             uint32_t read_len, uint32_t naive_start, uint32_t naive_end,
+                             uint32_t q_a, uint32_t q_b, int minus, const orc_lib_entry *lib,
+                             uint64_t n_lib, const orc_splice_params *sp, orc_junction *out,
+                             int *signal, uint32_t *support);
+int orc_intron_chain(const orc_contig *c, uint32_t contig_id, const uint8_t *read,
+                     uint32_t len, const orc_frag *left, const orc_frag *right,
+                     uint32_t pair_intron_start, uint32_t pair_intron_end, int minus,
+                     const orc_lib_entry *lib, uint64_t n_lib, const orc_intron_params *ip,
+                     const orc_params *p, orc_intron_out *out);
+
 /* ---- spliced pseudo-reference DP, crates/map/src/splice.rs ---- */
 uint32_t orc_stitch_cigar(const uint32_t *ops, uint32_t n_ops, uint32_t p_start,
                           const uint32_t *bounds, uint32_t n_bounds, const uint32_t *jlen,

@@ -206,7 +206,8 @@ def test_wide_reads_match_the_i32_flavour():
     assert max(O.run_band(c[0], c[1], wide=True, band=c[2])[0].score for c in cases) > 32767
     # extend_hint on long reads (both attempts in the wide kernel)
     for read, win, band, d in cases[:5]:
-        want = O.extend_hint(read, win, O.Params(edit_dir=d), offset=band[0] if band else 0)
+        want = O.extend_hint(read, win, O.Params(edit_dir=d), offset=band[0] if band else 0,
+                             wide=True)
         got = E.extend_hint(read, win, E.ExtendParams(edit_dir=d),
                             hint=E.DiagHint(band[0] if band else 0))
         assert got.key() == want.key(), (len(read), d)
@@ -223,8 +224,8 @@ def test_wide_reads_match_the_i32_flavour():
                 if mode == B.MODE_BAND:
                     want = O.run_band(read, win, O.Params(), wide=True, band=band)[0].key()
                 else:
-                    want = O.extend_hint(read, win, O.Params(),
-                                         offset=band[0] if band else 0).key()
+                    want = O.extend_hint(read, win, O.Params(), offset=band[0] if band else 0,
+                                         wide=True).key()
                 assert got[k][0] == want, (kern, mode, k, len(read))
 
 
