@@ -437,6 +437,7 @@ int esp_destroy(esp_handle *h) {
     cudaFree(h->d_my);
     cudaFree(h->d_spl);
     cudaFree(h->d_spl_io);
+    cudaFree(h->d_int);
     if (h->h_my) cudaFreeHost(h->h_my);
     cudaFree(h->d_hist);
     cudaFree(h->d_order);

@@ -82,6 +82,8 @@ struct esp_handle {
     size_t d_spl_cap = 0;
     void *d_spl_io = nullptr;   // host-API staging of reads / candidates / results
     size_t d_spl_io_cap = 0;
+    void *d_int = nullptr;      // intron-chain batch staging
+    size_t d_int_cap = 0;
     // Myers per-call / batch staging
     void *d_my = nullptr;
     size_t d_my_cap = 0;
@@ -220,3 +222,13 @@ void dp_scratch_bytes(esp_handle *h, int mode, uint64_t n_pairs, const Limits &L
 // batches of up to max_pairs pairs (abi.cu), so later batches of that size
 // allocate nothing but their DP scratch.
 int reserve_lists(esp_handle *h, uint64_t max_pairs);
+
+// The spliced pseudo-reference DP over exon slices (spliced.cu): gather the
+// pseudo-references from the genome, extend_hint along each read's hint
+// diagonal (hint_offset[r], or 0 when null), stitch back to the genome.
+int spliced_batch(esp_handle *h, const esp_genome *g, const esp_spliced_read *reads, uint64_t n,
+                  const uint8_t *read_arena, uint64_t read_arena_bytes,
+                  const esp_n_interval *read_iv, uint64_t n_read_iv, const esp_exon *exons,
+                  uint64_t n_exons, const esp_extend_params *params, const int64_t *hint_offset,
+                  esp_spliced_result *out, uint32_t *ext_cigar, uint32_t *stitched_cigar,
+                  uint32_t cigar_stride);

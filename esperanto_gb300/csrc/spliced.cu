@@ -7,7 +7,9 @@
 // handle's stream: (1) gather -- one thread per read packs its
 // pseudo-reference (the concatenated slices, 2-bit) from the genome into a
 // private, 16-byte-aligned stretch of a scratch arena; (2) the batched
-// extend_hint DP along the direct diagonal against it; (3) stitch -- one
+// extend_hint DP against it along the read's hint diagonal (the direct
+// diagonal for align_spliced; the intron-chain fast path passes its own
+// per read, spliced_batch); (3) stitch -- one
 // thread per read maps the pseudo-reference CIGAR back to the genome,
 // inserting an intron of exons[i+1].start - exons[i].end at every seam, and
 // the pseudo start back to a genomic start.
@@ -159,14 +161,12 @@ __global__ void spliced_stitch(const SplicedDev *__restrict__ R, uint64_t n,
 
 }  // namespace
 
-extern "C" int esp_batch_spliced_host(esp_handle *h, const esp_genome *g,
-                                      const esp_spliced_read *reads, uint64_t n,
-                                      const uint8_t *read_arena, uint64_t read_arena_bytes,
-                                      const esp_n_interval *read_iv, uint64_t n_read_iv,
-                                      const esp_exon *exons, uint64_t n_exons,
-                                      const esp_extend_params *params, esp_spliced_result *out,
-                                      uint32_t *ext_cigar, uint32_t *stitched_cigar,
-                                      uint32_t cigar_stride) {
+int spliced_batch(esp_handle *h, const esp_genome *g, const esp_spliced_read *reads, uint64_t n,
+                  const uint8_t *read_arena, uint64_t read_arena_bytes,
+                  const esp_n_interval *read_iv, uint64_t n_read_iv, const esp_exon *exons,
+                  uint64_t n_exons, const esp_extend_params *params, const int64_t *hint_offset,
+                  esp_spliced_result *out, uint32_t *ext_cigar, uint32_t *stitched_cigar,
+                  uint32_t cigar_stride) {
     if (!h || !g || !params || (n && (!reads || !read_arena || !exons || !out || !ext_cigar ||
                                       !stitched_cigar)) ||
         (n_read_iv && !read_iv))
@@ -206,7 +206,10 @@ extern "C" int esp_batch_spliced_host(esp_handle *h, const esp_genome *g,
         P.read_len = R.read_len;
         P.win_pos = pseudo_bases;
         P.win_len = (uint32_t)total;
-        P.band_offset = 0;
+        const int64_t off = hint_offset ? hint_offset[r] : 0;
+        if (off < -(1ll << 30) || off > (1ll << 30))
+            return fail(h, ESP_EDOMAIN, "hint offset out of range");
+        P.band_offset = (int32_t)off;
         P.band_half = 30;
         P.n_first = (uint32_t)iv.size();
         for (uint32_t q = 0; q < R.n_read; q++) iv.push_back(read_iv[R.n_first + q]);
@@ -277,4 +280,17 @@ extern "C" int esp_batch_spliced_host(esp_handle *h, const esp_genome *g,
     CK(h, cudaMemcpyAsync(stitched_cigar, b + o_sc, n * (size_t)cigar_stride * 4, cudaMemcpyDeviceToHost, st));
     CK(h, cudaStreamSynchronize(st));
     return ESP_OK;
+}
+
+extern "C" int esp_batch_spliced_host(esp_handle *h, const esp_genome *g,
+                                      const esp_spliced_read *reads, uint64_t n,
+                                      const uint8_t *read_arena, uint64_t read_arena_bytes,
+                                      const esp_n_interval *read_iv, uint64_t n_read_iv,
+                                      const esp_exon *exons, uint64_t n_exons,
+                                      const esp_extend_params *params, esp_spliced_result *out,
+                                      uint32_t *ext_cigar, uint32_t *stitched_cigar,
+                                      uint32_t cigar_stride) {
+    // align_spliced runs extend_hint along the direct diagonal (offset 0)
+    return spliced_batch(h, g, reads, n, read_arena, read_arena_bytes, read_iv, n_read_iv, exons,
+                         n_exons, params, nullptr, out, ext_cigar, stitched_cigar, cigar_stride);
 }

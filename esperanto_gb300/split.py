@@ -325,3 +325,68 @@ def channel_a_batch(genome: Genome, reads: np.ndarray, read_arena: np.ndarray,
     buf.check(rc)
     cells = int(N.lib().esp_last_cells(buf.handle))
     return out, cig[:len(reads) * cigar_stride].reshape(len(reads), cigar_stride), cells
+
+
+# ---- intron-chain fast path (intron_chain.rs:392-538 from the best pair on) ----
+
+FRAG_DTYPE = [("q_lo", "<u4"), ("q_hi", "<u4"), ("r_lo", "<u4"), ("r_hi", "<u4"),
+              ("n_anchors", "<u4")]
+INTRON_READ_DTYPE = np.dtype([("read_pos", "<u8"), ("read_len", "<u4"), ("contig", "<u4"),
+                              ("n_first", "<u4"), ("n_read", "<u4"), ("minus", "<i4"),
+                              ("intron_start", "<u4"), ("intron_end", "<u4"),
+                              ("left", FRAG_DTYPE), ("right", FRAG_DTYPE), ("pad", "<u4")])
+LIB_JUNCTION_DTYPE = np.dtype([("contig", "<u4"), ("start", "<u4"), ("end", "<u4"),
+                               ("minus_strand", "<i4"), ("count", "<u4")])
+INTRON_RES_DTYPE = np.dtype([("found", "<i4"), ("stage", "<i4"), ("donor_end", "<u4"),
+                             ("acceptor_start", "<u4"), ("verify_donor", "<i4"),
+                             ("verify_acceptor", "<i4"), ("j_contig", "<u4"), ("j_start", "<u4"),
+                             ("j_end", "<u4"), ("j_minus", "<i4"), ("signal", "<i4"),
+                             ("support", "<u4"), ("left_start", "<u4"), ("right_end", "<u4"),
+                             ("ext", B.EXT_DTYPE), ("genomic_start", "<u4"), ("n_ops", "<u4"),
+                             ("status", "<i4")])
+assert INTRON_READ_DTYPE.itemsize == 80 and INTRON_RES_DTYPE.itemsize == 100
+IC_STAGES = ("found", "empty", "anchors", "intron", "verify", "junction", "bounds", "result")
+
+
+@dataclass
+class IntronParams:
+    """intron_chain.rs:21-41 IntronParams::default()."""
+    min_frag_cov: int = 15
+    refine_window: int = 30
+    refine_pattern_len: int = 50
+    intron_max: int = 105_000
+
+
+def intron_chain_batch(genome: Genome, reads: np.ndarray, read_arena: np.ndarray,
+                       junction_lib: np.ndarray, read_n_iv: Optional[np.ndarray] = None,
+                       params: IntronParams = IntronParams(),
+                       extend_params: ExtendParams = ExtendParams(), cigar_stride: int = 64,
+                       buf: Optional[ExtendBuffer] = None):
+    """try_intron_chain_placement over a batch of reads with their best
+    fragment pairs: (results, extension CIGARs, stitched CIGARs)."""
+    buf = buf or genome.buf
+    reads = np.ascontiguousarray(reads, INTRON_READ_DTYPE)
+    read_arena = np.ascontiguousarray(read_arena, np.uint8)
+    lib = np.ascontiguousarray(junction_lib, LIB_JUNCTION_DTYPE)
+    iv = (np.zeros(0, B.NIV_DTYPE) if read_n_iv is None
+          else np.ascontiguousarray(read_n_iv, B.NIV_DTYPE))
+    n = len(reads)
+    out = np.zeros(n, INTRON_RES_DTYPE)
+    ec = np.zeros(max(1, n * cigar_stride), np.uint32)
+    sc = np.zeros(max(1, n * cigar_stride), np.uint32)
+    ip = (C.c_uint32 * 4)(params.min_frag_cov, params.refine_window, params.refine_pattern_len,
+                          params.intron_max)
+    p = extend_params._c()
+    L = N.lib()
+    fn = L.esp_batch_intron_chain_host
+    fn.argtypes = [C.c_void_p] * 3 + [C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                                      C.c_void_p, C.c_uint64, C.c_void_p,
+                                      C.POINTER(N.ExtendParamsC), C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_uint32]
+    rc = fn(buf.handle, genome.handle, reads.ctypes.data, n, read_arena.ctypes.data,
+            len(read_arena), iv.ctypes.data if len(iv) else None, len(iv),
+            lib.ctypes.data if len(lib) else None, len(lib), ip, C.byref(p), out.ctypes.data,
+            ec.ctypes.data, sc.ctypes.data, cigar_stride)
+    buf.check(rc)
+    return (out, ec[:n * cigar_stride].reshape(n, cigar_stride),
+            sc[:n * cigar_stride].reshape(n, cigar_stride))

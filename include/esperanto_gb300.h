@@ -466,6 +466,83 @@ int esp_batch_spliced_host(esp_handle *h, const esp_genome *g, const esp_spliced
                            const esp_extend_params *params, esp_spliced_result *out,
                            uint32_t *ext_cigar, uint32_t *stitched_cigar, uint32_t cigar_stride);
 
+/* ---- intron-chain fast path: crates/map/src/intron_chain.rs ----
+ *
+ * try_intron_chain_placement (intron_chain.rs:392-538) from the best
+ * fragment pair on, for a batch of reads (each in alignment orientation,
+ * with the pair best_frag_pair chose): the junction offset, EA-Myers
+ * breakpoint refinement of both sides (refine_donor_end /
+ * refine_acceptor_start, :285-343), split-read verification
+ * (verify_split_read, :347-373), the anchor / intron-length / mismatch-rate
+ * gates, read-aware junction refinement against the junction library
+ * (splice.rs:208-313 refine_junction_read; the pair's own junction when it
+ * finds none), the pseudo-reference extend_hint along the fragment's
+ * diagonal and stitch_cigar, and the final gates -- on the device over the
+ * resident genome.  The MEM extension, clustering and pair choice before it
+ * are seeding. */
+typedef struct {         /* intron_chain.rs:69-86 Frag: spans and MEM count */
+    uint32_t q_lo, q_hi; /* read span [q_lo, q_hi) */
+    uint32_t r_lo, r_hi; /* reference span [r_lo, r_hi) */
+    uint32_t n_anchors;
+} esp_frag;
+
+typedef struct {
+    uint64_t read_pos;     /* base offset in the read arena */
+    uint32_t read_len;
+    uint32_t contig;       /* the fragments' contig */
+    uint32_t n_first;      /* the read's N intervals */
+    uint32_t n_read;
+    int32_t minus;         /* the fragments' strand is minus */
+    uint32_t intron_start; /* best_frag_pair's intron: the fallback junction */
+    uint32_t intron_end;
+    esp_frag left, right;
+    uint32_t pad;
+} esp_intron_read;
+
+typedef struct {         /* intron_chain.rs:21-41 IntronParams (defaults 15, 30, 50, 105000) */
+    uint32_t min_frag_cov, refine_window, refine_pattern_len, intron_max;
+} esp_intron_params;
+
+typedef struct {         /* a JunctionLib entry (gtf.rs:72-149): sorted by (contig, start, end, strand) */
+    esp_junction j;
+    uint32_t count;
+} esp_lib_junction;
+
+#define ESP_IC_FOUND 0     /* Some(SplicedAlignment) */
+#define ESP_IC_EMPTY 1     /* empty read */
+#define ESP_IC_ANCHORS 2   /* fewer than two anchors */
+#define ESP_IC_INTRON 3    /* refined intron length outside [20, intron_max] */
+#define ESP_IC_VERIFY 4    /* split-read verification over the mismatch-rate thresholds */
+#define ESP_IC_JUNCTION 5  /* chosen junction outside [20, intron_max] */
+#define ESP_IC_BOUNDS 6    /* the exon bounds do not enclose the junction */
+#define ESP_IC_RESULT 7    /* non-positive score, a CIGAR that loses read bases or has no intron */
+
+typedef struct {
+    int32_t found;
+    int32_t stage;           /* ESP_IC_*: the gate that ended the read */
+    uint32_t donor_end;      /* refine_donor_end */
+    uint32_t acceptor_start; /* refine_acceptor_start */
+    int32_t verify_donor;    /* verify_split_read distances (INT32_MAX when skipped) */
+    int32_t verify_acceptor;
+    esp_junction junction;   /* the refined junction */
+    int32_t signal;          /* ESP_SIG_* */
+    uint32_t support;        /* library support of the junction */
+    uint32_t left_start;     /* exon bounds: (0, left_start, junction.start), */
+    uint32_t right_end;      /* (junction.start - left_start, junction.end, right_end) */
+    esp_extension ext;       /* extend_hint against the pseudo-reference */
+    uint32_t genomic_start;  /* SplicedAlignment::genomic_start */
+    uint32_t n_ops;          /* stitched CIGAR ops */
+    int32_t status;          /* ESP_OK, or ESP_ECAP when a CIGAR exceeds the stride */
+} esp_intron_result;
+
+int esp_batch_intron_chain_host(esp_handle *h, const esp_genome *g, const esp_intron_read *reads,
+                                uint64_t n, const uint8_t *read_arena, uint64_t read_arena_bytes,
+                                const esp_n_interval *read_iv, uint64_t n_read_iv,
+                                const esp_lib_junction *lib, uint64_t n_lib,
+                                const esp_intron_params *ip, const esp_extend_params *params,
+                                esp_intron_result *out, uint32_t *ext_cigar,
+                                uint32_t *stitched_cigar, uint32_t cigar_stride);
+
 /* ---- strict rescoring: crates/map/src/align.rs:1060-1165 rescore_with ----
  *
  * One record per placement: its query (ASCII, compared byte for byte as the
