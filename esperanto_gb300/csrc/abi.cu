@@ -391,6 +391,12 @@ int esp_create(esp_handle **out, int device) {
     esp_handle *h = new (std::nothrow) esp_handle();
     if (!h) return ESP_ENOMEM;
     h->device = device;
+    // DP scratch one launch may use: ESP_SCRATCH_BUDGET bytes, else 8 GiB
+    // (fewer resident warps when a batch's geometry needs more)
+    if (const char *v = getenv("ESP_SCRATCH_BUDGET")) {
+        const unsigned long long b = strtoull(v, nullptr, 10);
+        if (b >= (1ull << 20)) h->scratch_budget = b;
+    }
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);

@@ -730,14 +730,21 @@ int esp_chunk_destroy(esp_chunk *c);
  *     esp_batch_extend_device; the call is asynchronous on `stream`
  *     (NULL = legacy default stream) on the current device.
  *   - The first call on a device looks up the array's device address for
- *     that device; make that first call before any stream capture.
+ *     that device and keeps it for the process; make that first call before
+ *     any stream capture, and do not call it after cudaDeviceReset (the
+ *     address kept would belong to the destroyed context).
  *   - Every call shares the one array: calls that can overlap on the GPU
  *     (different streams, different host threads) race and must be
  *     serialised by the caller.
  *   - Work whose per-block scratch (4 warps x 32 pairs of traceback and
  *     row-buffer words, sized from `limits`) exceeds the array returns
- *     ESP_ESCRATCH; smaller work runs with fewer resident blocks when the
- *     array cannot hold a full persistent grid.
+ *     ESP_ESCRATCH, whatever n_pairs is (even a batch of a few pairs needs
+ *     one block's scratch); smaller work runs with fewer resident blocks
+ *     when the array cannot hold a full persistent grid, each thread taking
+ *     pairs from the queue in turn.
+ *   - Reads longer than the int16 domain (8191 / largest substitution
+ *     score) are refused (ESP_EDOMAIN): the wide kernel needs scratch sized
+ *     per pair.
  *   - Pairs run in the order given (no length binning). */
 #define ESP_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int esp_batch_run_band_noalloc(const esp_pair *pairs, uint64_t n_pairs, const uint8_t *arena,

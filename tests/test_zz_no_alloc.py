@@ -117,3 +117,63 @@ def test_noalloc_rejects_work_beyond_its_scratch():
                                       C.byref(lim), C.byref(p), dummy.data_ptr(),
                                       dummy.data_ptr(), 1, None)
     assert rc == ESP_ESCRATCH
+
+
+def test_noalloc_reuses_scratch_slots_and_allocates_nothing():
+    """About 2,000 full-matrix pairs of ~300 x 600 bases: one block's scratch
+    is ~12 MB, so the fixed array holds only five blocks and every thread
+    takes several pairs from the queue in turn, reusing its scratch slot.
+    Two calls in a row equal the regular entry point, and the second call
+    (after the first has done the per-device set-up) leaves the device's
+    free memory unchanged: no handle, no allocation."""
+    L = _lib()
+    rng = np.random.default_rng(9)
+    reads, wins = [], []
+    for k in range(2000):
+        n = int(rng.integers(560, 601))
+        m = int(rng.integers(260, 301))
+        win = rng.choice(list("ACGT"), n)
+        s = int(rng.integers(0, n - m))
+        read = list(win[s:s + m])
+        for q in rng.choice(m, 6, replace=False):
+            read[int(q)] = str(rng.choice(list("ACGT")))
+        reads.append("".join(read).encode())
+        wins.append("".join(win).encode())
+    arena, pairs, n_iv = B.pack_ascii_pairs(reads, wins, [0] * len(reads), [-1] * len(reads))
+    n = len(pairs)
+    stride = 48
+    lim = N.BatchLimitsC(int(pairs["read_len"].max()), int(pairs["win_len"].max()), -1)
+    p = ExtendParams()._c()
+    d_arena, d_pairs = _dev(arena), _dev(pairs)
+    buf = ExtendBuffer()
+    ref_out = torch.zeros(n * B.EXT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    ref_cig = torch.zeros(n * stride, dtype=torch.int32, device="cuda")
+    buf.check(L.esp_batch_extend_device(buf.handle, B.MODE_BAND, d_pairs.data_ptr(), n,
+                                        d_arena.data_ptr(), arena.nbytes, None, 0, C.byref(lim),
+                                        C.byref(p), ref_out.data_ptr(), ref_cig.data_ptr(),
+                                        stride, None))
+    torch.cuda.synchronize()
+    want = ref_out.cpu().numpy().view(B.EXT_DTYPE)
+    want_cig = ref_cig.cpu().numpy().reshape(n, stride)
+    assert (want["status"] == 0).all()
+    out = torch.zeros(n * B.EXT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    cig = torch.zeros(n * stride, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for call in range(2):
+        out.zero_()
+        cig.zero_()
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
+        rc = L.esp_batch_run_band_noalloc(d_pairs.data_ptr(), n, d_arena.data_ptr(),
+                                          arena.nbytes, None, 0, C.byref(lim), C.byref(p),
+                                          out.data_ptr(), cig.data_ptr(), stride, stream)
+        assert rc == 0, f"call {call}: status {rc}"
+        torch.cuda.synchronize()
+        if call == 1:
+            assert torch.cuda.mem_get_info()[0] == free_before
+        got = out.cpu().numpy().view(B.EXT_DTYPE)
+        got_cig = cig.cpu().numpy().reshape(n, stride)
+        assert np.array_equal(got, want), f"call {call}"
+        for k in range(n):
+            k_ops = int(want[k]["n_ops"])
+            assert np.array_equal(got_cig[k, :k_ops], want_cig[k, :k_ops]), (call, k)
