@@ -566,6 +566,79 @@ def serve_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def other_config(config, args, local, torch):
+    """A short, clocked measurement of another workload for the default line:
+    the 150 x 214 banded batch (0), the EA-Myers batch (1) or the split-read
+    rescue (3), each at its full size with inputs resident, end to end
+    through the host batch API, on its own integer roofline and next to the
+    oracle port on the host cores."""
+    from esperanto_gb300 import _native as N
+    from esperanto_gb300.extend import ExtendBuffer
+    L = N.lib()
+    dev = f"cuda:{local}"
+    wl = make_workload(config)
+    n = DEFAULT_PAIRS[config]
+    seed = SEEDS[config]
+    buf = ExtendBuffer(local)
+    stream = torch.cuda.ExternalStream(buf.stream_ptr())
+    wl.setup(seed, n, dev, buf, torch)
+    for _ in range(3):
+        wl.step()
+    torch.cuda.synchronize()
+    bad = int((wl.result_status() != 0).sum())
+    steps = 3 if config == 3 else 10
+    clk = ClockSampler()
+    clk.start()
+    t_clk = time.perf_counter()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    with torch.cuda.stream(stream):
+        evs[0].record(stream)
+        for _ in range(steps):
+            wl.step()
+        evs[1].record(stream)
+    torch.cuda.synchronize()
+    while time.perf_counter() - t_clk < 0.6:  # let the 200 ms samples see the load
+        wl.step()
+        torch.cuda.synchronize()
+    clocks = clk.stop(local)
+    ms = evs[0].elapsed_time(evs[1]) / steps
+    launches = int(L.esp_last_launch_count(buf.handle)) * steps
+    e2e_ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        wl.e2e_step()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    lanes = getattr(wl, "lanes", 1)
+    peak_ops, _ = int_peak(local, lanes)
+    achieved = wl.cells * wl.ops_per_cell / (ms / 1e3)
+    out = {"workload": wl.describe(n), "metric": "GCUPS",
+           "value": wl.cells / (ms / 1e3) / 1e9, "unit": "GCUPS", "ms_per_step": ms,
+           "steps": steps, "warmup": 3, "pairs_per_s": n / (ms / 1e3), "dtype": wl.dtype,
+           "cells_per_step": wl.cells, "bad_status": bad, "gpu_launches": launches,
+           "e2e": {"value": wl.cells / (float(np.median(e2e_ms)) / 1e3) / 1e9, "unit": "GCUPS",
+                   "h2d_bytes_per_step": int(wl.h2d), "d2h_bytes_per_step": int(wl.d2h),
+                   "statistic": "median of 3 steps"},
+           "roofline": {"bound": "int_alu", "achieved": achieved / 1e12,
+                        "peak": peak_ops / 1e12, "unit": "Tops/s", "frac": achieved / peak_ops,
+                        "ops_per_cell": wl.ops_per_cell, "simd_lanes": lanes},
+           "clocks": clocks}
+    if config == 0:
+        out["extend_hint"] = wl.hint_measure(buf, torch, stream)
+    if config == 3:
+        out["candidates"] = wl.n_cands
+        out["rescued"] = wl.found
+    if not args.no_cpu_baseline:
+        run, sample = wl.cpu_reference(seed, args.cpu_sample, os.cpu_count() or 1)
+        run()
+        c, dt = run()
+        out["cpu_baseline"] = {"value": c / dt / 1e9, "unit": "GCUPS",
+                               "cores": os.cpu_count() or 1, "kind": "port", "sample": sample}
+    del wl
+    buf.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def make_workload(config):
     if config == 1:
         return MyersWorkload()
@@ -635,6 +708,8 @@ def main():
                     help="seconds at each of 70%% and 80%% of peak in the serve phase")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the serve phase of the default (mixed-length) line")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the other workloads' measurements in the default line")
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--e2e-steps", type=int, default=8)
@@ -792,6 +867,9 @@ def main():
         # callers run (align.rs:1907): its escalation rate is how often the
         # two-attempt policy runs twice
         line["extend_hint"] = wl.hint_measure(buf, torch, stream)
+    if config == 2 and not args.no_others and world == 1:
+        # the other batched workloads, each clocked, at full size
+        line["other_configs"] = {str(c): other_config(c, args, local, torch) for c in (0, 1, 3)}
     if config == 2 and not args.no_serve and world == 1:
         # the serving loop (continuous batching over a resident genome),
         # with its own clock record
