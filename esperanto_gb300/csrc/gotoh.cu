@@ -405,6 +405,21 @@ struct Walker {
         } else {
             nk = -1;
         }
+        // L2 prefetch of the word 8 diagonal steps ahead (the lane-interleaved
+        // global traceback of the thread kernels): the walk mostly runs
+        // along the diagonal, and the lines it reads have left L2 since the
+        // fill wrote them
+        if (TBS == 32) {
+            const int pi = i - 8, pj = j - 8;
+            if (pi >= 1 && pj >= 1) {
+                const int ps = (pi - 1) >> 3;
+                const int pclo = ps == s ? cclo : g.lo(ps * STRIP + 1);
+                if (pj >= pclo) {
+                    const uint32_t *pa = tb + (size_t)((int64_t)ps * sw + (pj - pclo)) * TBS;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pa));
+                }
+            }
+        }
         int sh = 2 * (7 - r);
         uint32_t hsrc = (w >> sh) & 3u;
         uint32_t eo = (w >> (16 + sh)) & 1u;
