@@ -34,6 +34,7 @@
 // as the scalar kernel's margins do (extend.rs:718-759).
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstdint>
 #include <type_traits>
 
@@ -477,24 +478,46 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
                           const Seq &win, const FillResult &F, esp_extension &o, uint32_t *cig,
                           uint32_t cap) {
     const int dtab[7] = {K.match, (int)K.lut[1], 0, K.open_ext, K.ext, K.open_ext, K.ext};
+    // Walk 1 records each 8-step block of the walk: its steps' kinds (rec),
+    // the prefix sum before it (pst) and its largest prefix sum (bmx), so
+    // that the trim below finds its cut by blocks instead of re-walking.
     uint32_t rec[REC_WORDS];
-    // walk 1: number of steps N, total T, trail; steps recorded for walk 2
-    int N = 0, P = 0, trail = 0;
+    int pst[REC_WORDS], bmx[REC_WORDS];
+    // walk 1: number of steps N, total T, trail (with the prefix sum before
+    // step `trail` and the cell the walk stood on there)
+    int N = 0, P = 0, trail = 0, ptrail = 0, tr_i = F.best_i, tr_j = F.best_j;
     {
         Walker<TBS> W(g, tb, sw, read, win, K, F.best_i, F.best_j);
         int kind;
         uint32_t acc = 0;
+        int bm = INT_MIN, pb = 0;
         while (W.step(kind)) {
             P += dtab[kind];
+            bm = max(bm, P);
             acc |= (uint32_t)kind << (4 * (N & 7));
             N++;
             if ((N & 7) == 0) {
-                if ((N >> 3) <= REC_WORDS) rec[(N >> 3) - 1] = acc;
+                if ((N >> 3) <= REC_WORDS) {
+                    rec[(N >> 3) - 1] = acc;
+                    pst[(N >> 3) - 1] = pb;
+                    bmx[(N >> 3) - 1] = bm;
+                }
                 acc = 0;
+                bm = INT_MIN;
+                pb = P;
             }
-            if (P <= 0) trail = N;
+            if (P <= 0) {
+                trail = N;
+                ptrail = P;
+                tr_i = W.i;
+                tr_j = W.j;
+            }
         }
-        if ((N & 7) && (N >> 3) < REC_WORDS) rec[N >> 3] = acc;
+        if ((N & 7) && (N >> 3) < REC_WORDS) {
+            rec[N >> 3] = acc;
+            pst[N >> 3] = pb;
+            bmx[N >> 3] = bm;
+        }
     }
     const bool replay = N <= REC_WORDS * 8;
     const int T = P;
@@ -523,13 +546,89 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
         ref_start = (uint32_t)max(F.best_j, 0);
         read_end = read_start;
         ref_end = ref_start;
+    } else if (replay) {
+        // With walk-order prefix sums P_t, the reference's forward lead is
+        // N-1-u where u is the first index in [-1, N-2] with P_u >= T
+        // (P_-1 = 0): the first block whose largest prefix sum reaches T
+        // holds it (the last block always does, through P_N-1 = T, but
+        // only its steps up to N-2 count).  The kept steps are walk indices
+        // [trail, u] -- through N-1 when no u exists -- and lead + trail >=
+        // N (the degenerate keep-the-middle case, extend.rs:956-960) is
+        // exactly u < trail, or T <= 0.
+        int ue = N - 1, Pue = T;
+        bool degenerate = T <= 0;
+        if (!degenerate) {
+            const int nb = (N + 7) >> 3;
+            for (int b = 0; b < nb; b++) {
+                if (bmx[b] < T) continue;
+                int Pb = pst[b];
+                uint32_t w = rec[b];
+                const int tend = min(8 * b + 7, N - 2);
+                int t = 8 * b;
+                for (; t <= tend; t++, w >>= 4) {
+                    Pb += dtab[w & 15u];
+                    if (Pb >= T) break;
+                }
+                if (t <= tend) {
+                    ue = t;
+                    Pue = Pb;
+                    degenerate = t < trail;
+                }
+                break;
+            }
+        }
+        if (degenerate) {  // the middle step t* = N-1-N/2 alone
+            const int tstar = N - 1 - N / 2;
+            int i = F.best_i, j = F.best_j, op = 0, d = 0;
+            for (int t = 0; t <= tstar; t++) {
+                const int kind = (int)((rec[t >> 3] >> (4 * (t & 7))) & 15u);
+                op = kind_op(kind);
+                d = dtab[kind];
+                if (t == tstar) break;
+                if (op != ESP_OP_D) i--;
+                if (op != ESP_OP_I) j--;
+            }
+            read_end = (uint32_t)i;
+            ref_end = (uint32_t)j;
+            read_start = (uint32_t)(op != ESP_OP_D ? i - 1 : i);
+            ref_start = (uint32_t)(op != ESP_OP_I ? j - 1 : j);
+            score = d;
+            emit((1u << 4) | (uint32_t)op);
+            first_op = last_op = op;
+        } else {
+            // runs of steps [trail, ue] in walk order; the kept region ends
+            // (forward order) where the walk stood before step `trail`
+            read_end = (uint32_t)tr_i;
+            ref_end = (uint32_t)tr_j;
+            uint32_t w = rec[trail >> 3] >> (4 * (trail & 7));
+            last_op = kind_op((int)(w & 15u));
+            int cur_op = last_op;
+            uint32_t cur_len = 0, di = 0, dj = 0;
+            for (int t = trail; t <= ue; t++) {
+                if ((t & 7) == 0) w = rec[t >> 3];
+                const int op = kind_op((int)(w & 15u));
+                w >>= 4;
+                if (op != cur_op) {
+                    emit((cur_len << 4) | (uint32_t)cur_op);
+                    if (cur_op != ESP_OP_D) di += cur_len;
+                    if (cur_op != ESP_OP_I) dj += cur_len;
+                    cur_op = op;
+                    cur_len = 0;
+                }
+                cur_len++;
+            }
+            emit((cur_len << 4) | (uint32_t)cur_op);
+            if (cur_op != ESP_OP_D) di += cur_len;
+            if (cur_op != ESP_OP_I) dj += cur_len;
+            first_op = cur_op;
+            read_start = read_end - di;
+            ref_start = ref_end - dj;
+            score = Pue - ptrail;
+        }
     } else {
-        // Walk 2.  With walk-order prefix sums P_t, the reference's forward
-        // lead is N-1-u where u is the first index in [-1, N-2] with
-        // P_u >= T (P_-1 = 0), so the kept steps are walk indices
-        // [trail, u]; lead + trail >= N (the degenerate keep-the-middle
-        // case, extend.rs:956-960) is exactly u < trail.  Step t* (the
-        // middle step) is captured on the way in case that happens.
+        // Walks longer than the record: walk 2 re-walks the traceback,
+        // finding u (as above) on the way.  Step t* (the middle step) is
+        // captured in case the degenerate case comes up.
         bool degenerate = (T <= 0);  // u = -1
         const int tstar = N - 1 - N / 2;
         Walker<TBS> W(g, tb, sw, read, win, K, F.best_i, F.best_j);
@@ -544,8 +643,7 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
         for (int t = 0; t < N && !done; t++) {
             int i_before = i, j_before = j;
             int kind;
-            if (replay) kind = (int)((rec[t >> 3] >> (4 * (t & 7))) & 15u);
-            else W.step(kind);
+            W.step(kind);
             int op = kind_op(kind), d = dtab[kind];
             if (op != ESP_OP_D) i--;
             if (op != ESP_OP_I) j--;
