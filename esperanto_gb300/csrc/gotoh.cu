@@ -1007,6 +1007,8 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
         const bool handoff = lane == 31 && s + 1 < nstrips;
         int cw_at = -1000000;  // first window position of the cached code word
         uint32_t cw = 0, cn = 0;
+        int nx_at = -1000000;  // the word after it, loaded one word ahead
+        uint32_t nx = 0, nxn = 0;
         for (int t = t0; t <= t1; t++) {
             const int j = t - lane;
             int inH, inE;
@@ -1026,12 +1028,24 @@ __device__ FillResult warp_fill(const GotohConst &K, const uint32_t *__restrict_
             }
             int outH = 2, outE = NEG4;
             if (act && j >= clo && j <= chi) {
-                // window codes 16 at a time (a load per column would sit on
-                // the wavefront's critical path)
+                // window codes 16 at a time, each word loaded while the
+                // one before is in use: a load that a lane waits for stalls
+                // the whole wavefront, and the lanes reach their word
+                // boundaries at different steps
                 if (j - 1 >= cw_at + 16) {
+                    if (j - 1 == nx_at) {
+                        cw = nx;
+                        cn = nxn;
+                    } else {
+                        cw = load16(P.win.arena, P.win.pos + (uint64_t)(j - 1));
+                        cn = P.win.cnt ? nmask16(P.win.iv, P.win.cnt, j - 1) : 0u;
+                    }
                     cw_at = j - 1;
-                    cw = load16(P.win.arena, P.win.pos + (uint64_t)cw_at);
-                    cn = P.win.cnt ? nmask16(P.win.iv, P.win.cnt, cw_at) : 0u;
+                    nx_at = cw_at + 16;
+                    if (nx_at < n) {
+                        nx = load16(P.win.arena, P.win.pos + (uint64_t)nx_at);
+                        nxn = P.win.cnt ? nmask16(P.win.iv, P.win.cnt, nx_at) : 0u;
+                    }
                 }
                 const int sh = j - 1 - cw_at;
                 uint32_t code = ((cn >> (31 - sh)) & 1u) ? 4u : ((cw >> (30 - 2 * sh)) & 3u);
