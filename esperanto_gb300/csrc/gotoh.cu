@@ -352,32 +352,40 @@ struct Walker {
     int cs, cclo;          // current strip and its first column
     int64_t ck, nk;        // cached / prefetched word index
     uint32_t cw, nw;
-    int64_t rq, wq;        // first position of the cached code words
-    uint32_t rword, rnm, wword, wnm;
 
     __device__ Walker(const Geo &g_, const uint32_t *tb_, int sw_, const Seq &r_, const Seq &w_,
                       const GotohConst &K_, int bi, int bj)
         : g(g_), tb(tb_), sw(sw_), read(r_), win(w_), K(K_), i(bi), j(bj), state(0), cs(-1),
-          cclo(0), ck(-1), nk(-1), cw(0), nw(0), rq(-100), wq(-100), rword(0), rnm(0), wword(0),
-          wnm(0) {}
+          cclo(0), ck(-1), nk(-1), cw(0), nw(0) {}
 
-    __device__ __forceinline__ uint32_t rcode(int64_t q) {
-        if (q < rq || q >= rq + 16) {
-            rq = q >= 15 ? q - 15 : 0;
-            rword = load16(read.arena, read.pos + (uint64_t)rq);
-            rnm = read.cnt ? nmask16(read.iv, read.cnt, rq) : 0u;
-        }
-        int k = (int)(q - rq);
-        return ((rnm >> (31 - k)) & 1u) ? 4u : ((rword >> (30 - 2 * k)) & 3u);
+    // codes of read position i-1 and window position j-1 at bits 1:0 (N
+    // flag at bit 0 of rnb / wnb); rleft / wleft = positions below still
+    // in the register (< 0: reload)
+    uint32_t rv = 0, wv = 0, rnb = 0, wnb = 0;
+    int rleft = -1, wleft = -1;
+    __device__ __forceinline__ void rfill() {
+        const int q = i - 1, q0 = q >= 15 ? q - 15 : 0, k = q - q0;
+        rv = load16(read.arena, read.pos + (uint64_t)q0) >> (30 - 2 * k);
+        rnb = read.cnt ? nmask16(read.iv, read.cnt, q0) >> (31 - k) : 0u;
+        rleft = k;
     }
-    __device__ __forceinline__ uint32_t wcode(int64_t q) {
-        if (q < wq || q >= wq + 16) {
-            wq = q >= 15 ? q - 15 : 0;
-            wword = load16(win.arena, win.pos + (uint64_t)wq);
-            wnm = win.cnt ? nmask16(win.iv, win.cnt, wq) : 0u;
-        }
-        int k = (int)(q - wq);
-        return ((wnm >> (31 - k)) & 1u) ? 4u : ((wword >> (30 - 2 * k)) & 3u);
+    __device__ __forceinline__ void wfill() {
+        const int q = j - 1, q0 = q >= 15 ? q - 15 : 0, k = q - q0;
+        wv = load16(win.arena, win.pos + (uint64_t)q0) >> (30 - 2 * k);
+        wnb = win.cnt ? nmask16(win.iv, win.cnt, q0) >> (31 - k) : 0u;
+        wleft = k;
+    }
+    __device__ __forceinline__ void idec() {
+        i--;
+        rv >>= 2;
+        rnb >>= 1;
+        rleft--;
+    }
+    __device__ __forceinline__ void jdec() {
+        j--;
+        wv >>= 2;
+        wnb >>= 1;
+        wleft--;
     }
 
     // Take one step; returns false when the walk stops.  `kind` is the step.
@@ -425,36 +433,24 @@ struct Walker {
         uint32_t hsrc = (w >> sh) & 3u;
         uint32_t eo = (w >> (16 + sh)) & 1u;
         uint32_t fo = (w >> (17 + sh)) & 1u;
-        if (state == 0) {
-            if (hsrc == 2u) {
-                uint32_t q = rcode(i - 1), rc = wcode(j - 1);
-                if (q == rc && q < 4) kind = K_MM;
-                else if ((K.edit_dir == ESP_EDIT_AG && q == 2 && rc == 0) ||
-                         (K.edit_dir == ESP_EDIT_TC && q == 1 && rc == 3))
-                    kind = K_MZ;
-                else kind = K_MX;
-                i--;
-                j--;
-            } else if (hsrc == 1u) {
-                kind = K_IO;
-                state = eo ? 0 : 1;
-                i--;
-            } else if (hsrc == 0u) {
-                kind = K_DO;
-                state = fo ? 0 : 2;
-                j--;
-            } else {
-                return false;  // H_START
-            }
-        } else if (state == 1) {
-            kind = K_IE;
-            if (eo) state = 0;
-            i--;
-        } else {
-            kind = K_DE;
-            if (fo) state = 0;
-            j--;
-        }
+        // the step's source: the cell's H tag in state 0, else the gap it is in
+        const uint32_t eff = state == 0 ? hsrc : (state == 1 ? 1u : 0u);
+        if (eff == 3u) return false;  // H_START
+        if (rleft < 0) rfill();
+        if (wleft < 0) wfill();
+        const uint32_t q = (rnb & 1u) ? 4u : (rv & 3u), rc = (wnb & 1u) ? 4u : (wv & 3u);
+        // diagonal kinds K_MM 0 / K_MX 1 / K_MZ 2 without branches (a match
+        // and an edit-tolerated pair exclude each other)
+        const int mm = (q == rc) & (q < 4u);
+        const int mz = ((K.edit_dir == ESP_EDIT_AG) & (q == 2u) & (rc == 0u)) |
+                       ((K.edit_dir == ESP_EDIT_TC) & (q == 1u) & (rc == 3u));
+        const int open = state == 0;
+        const int kdiag = 1 - mm + mz;
+        const int kvert = open ? K_IO : K_IE, khor = open ? K_DO : K_DE;
+        kind = eff == 2u ? kdiag : (eff == 1u ? kvert : khor);
+        state = eff == 2u ? 0 : (eff == 1u ? (eo ? 0 : 1) : (fo ? 0 : 2));
+        if (eff != 0u) idec();
+        if (eff != 1u) jdec();
         return true;
     }
 };
