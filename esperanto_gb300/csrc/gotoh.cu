@@ -98,6 +98,13 @@ __device__ __forceinline__ uint32_t and_u32(uint32_t a, uint32_t m) {
     return d;
 }
 
+// (a | b) & m in one LOP3
+__device__ __forceinline__ uint32_t or_and_u32(uint32_t a, uint32_t b, uint32_t m) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0xA8;" : "=r"(d) : "r"(a), "r"(b), "r"(m));
+    return d;
+}
+
 __device__ __forceinline__ uint32_t and_or_u32(uint32_t a, uint32_t m, uint32_t o) {
     uint32_t d;
     asm("lop3.b32 %0, %1, %2, %3, 0xEA;" : "=r"(d) : "r"(a), "r"(m), "r"(o));
@@ -120,17 +127,17 @@ __device__ __forceinline__ uint32_t dp_column(StripT<WIDE> &S, const GotohConst 
         int left = S.Hl[r];
         int kE = max(upE + K.ex4, upH + K.oe1);
         int kF = max(S.Fl[r] + K.ex4, left + K.oe4);
-        // kE = 0 or 1 and kF = 0 or 2 (mod 4): the opened flags are kE - E4
-        // and kF - F4, the E tag is E4 + 1, the key's tag key - Hp + 2 --
-        // adds, which also issue on the FMA pipe, instead of logic ops on
-        // the saturated ALU pipe
+        // kE = 0 or 1 and kF = 0 or 2 (mod 4): the two opened flags are
+        // (kE | kF) & 3 (one LOP3); the E tag is E4 + 1 and the key's tag
+        // key - Hp + 2 -- adds, which also issue on the FMA pipe, instead of
+        // logic ops on the saturated ALU pipe
         int E4 = (int)and_u32((uint32_t)kE, ~3u);
         int F4 = (int)and_u32((uint32_t)kF, ~3u);
         int kd = max(d + prmt_sx(S.l0[r], S.l1[r], sel), 3);  // START tag 3 folded in
         int key = max(max(kd, E4 + 1), F4);
         int Hp = (int)and_or_u32((uint32_t)key, ~3u, 2u);
         wa = mad_u32(wa, 4u, (uint32_t)(key - Hp + 2));
-        wb = mad_u32(wb, 4u, (uint32_t)((kE - E4) + (kF - F4)));
+        wb = mad_u32(wb, 4u, or_and_u32((uint32_t)kE, (uint32_t)kF, 3u));
         typename StripT<WIDE>::RK rkey;
         if constexpr (WIDE)
             rkey = ((long long)Hp << 15) | (long long)cj;
@@ -1258,16 +1265,16 @@ __device__ __forceinline__ void dp_column2(Strip2 &S, const uint32_t oe1, const 
         uint32_t left = S.Hl[r];
         uint32_t kE = __viaddmax_s16x2(upE, ex4, __viaddmax_s16x2(upH, oe1, VNEG2));
         uint32_t kF = __viaddmax_s16x2(S.Fl[r], ex4, __viaddmax_s16x2(left, oe4, VNEG2));
-        // tags and flags by adds as in dp_column: every half's result is in
-        // [0, 3] (E4 + 1 cannot carry: E4's low bits are 0), so the packed
-        // 32-bit adds are exact per half
+        // tags by adds and flags by one LOP3 as in dp_column: every half's
+        // result is in [0, 3] (E4 + 1 cannot carry: E4's low bits are 0), so
+        // the packed 32-bit adds are exact per half
         uint32_t E4 = and_u32(kE, KEEP2);
         uint32_t F4 = and_u32(kF, KEEP2);
         uint32_t kd = __viaddmax_s16x2(d, prmt(S.la[r], S.lb[r], sel), 0x00030003u);
         uint32_t key = __vimax3_s16x2(kd, E4 + 0x00010001u, F4);
         uint32_t Hp = and_or_u32(key, KEEP2, 0x00020002u);
         wa = mad_u32(wa, 4u, key - Hp + 0x00020002u);
-        wb = mad_u32(wb, 4u, (kE - E4) + (kF - F4));
+        wb = mad_u32(wb, 4u, or_and_u32(kE, kF, 0x00030003u));
         if (MASK) {  // out-of-window cells: as in dp_column
             const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
             const bool in = (j >= lo) & (j <= hi);
