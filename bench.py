@@ -53,7 +53,7 @@ MYERS_OPS_PER_CELL = 10.0 / 32.0
 TRAFFIC_BYTES = {0: 51.8e6 + 348.4e6, 1: 125.5e6 + 9.3e6}
 # keyed by (workload, SIMD lanes): one pair per thread, two pairs per thread
 TRAFFIC_PER_CELL = {(2, 1): (2713001472 + 6431804160) / 7716062109,
-                    (2, 2): (34778164224 + 59818551296) / 61820954081}
+                    (2, 2): (35225117184 + 60432276480) / 61820954081}
 TRAFFIC_SOURCE = {0: "profiles/gotoh_kernel_banded150x214_65536pairs.md",
                   1: "profiles/myers_kernel_150x200_1048576pairs.md",
                   2: "profiles/gotoh_kernel_traffic_mixedlength.md (scaled by cells)"}
