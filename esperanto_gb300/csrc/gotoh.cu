@@ -346,7 +346,10 @@ __device__ __forceinline__ int kind_op(int k) { return k < 3 ? ESP_OP_M : (k < 5
 // H/E/F from (best_i, best_j), stopping at i <= 0, j <= 0, outside the row
 // window, or on an H START cell.  Word loads are cached and the word of the
 // next column is prefetched (most steps move one column left in the strip);
-// read and window codes are cached 16 bases at a time.
+// the read and window codes at the walk's position ride in shift registers
+// that move with it (reloaded 16 bases at a time), and each step's kind and
+// next state are chosen by selects, so that the lanes' walks, which take
+// different kinds of steps, do not split on branches.
 template <int TBS>
 struct Walker {
     const Geo &g;
