@@ -24,6 +24,7 @@ struct GotohConst {
     uint32_t lut4[5][2];  // per read code: bytes = 4*score vs ref codes 0..7 (4..7 = N)
     int8_t lut[25];       // SubstLut scores[read*5 + ref] (raw, for traceback deltas)
     int32_t max_m;        // longest read whose scores fit the int16 row buffer
+    uint64_t dkind;       // traceback kind of a diagonal step (2 bits) by read code * 5 + ref code
 };
 
 // Validate parameters against the device domain and fill the constants.

@@ -360,13 +360,14 @@ struct Walker {
     const GotohConst &K;
     int i, j, state;
     int cs, cclo;          // current strip and its first column
-    int64_t ck, nk;        // cached / prefetched word index
+    int pdelta, pmin;      // word index offset of (i-8, j-8) and the first j it exists for
+    int ck, nk;            // cached / prefetched word index
     uint32_t cw, nw;
 
     __device__ Walker(const Geo &g_, const uint32_t *tb_, int sw_, const Seq &r_, const Seq &w_,
                       const GotohConst &K_, int bi, int bj)
         : g(g_), tb(tb_), sw(sw_), read(r_), win(w_), K(K_), i(bi), j(bj), state(0), cs(-1),
-          cclo(0), ck(-1), nk(-1), cw(0), nw(0) {}
+          cclo(0), pdelta(0), pmin(0x7fffffff), ck(-1), nk(-1), cw(0), nw(0) {}
 
     // codes of read position i-1 and window position j-1 at bits 1:0 (N
     // flag at bit 0 of rnb / wnb); rleft / wleft = positions below still
@@ -406,21 +407,28 @@ struct Walker {
         if (s != cs) {
             cs = s;
             cclo = g.lo(s * STRIP + 1);
+            if (TBS == 32 && s > 0) {  // (i-8, j-8) lies in strip s-1, row r
+                const int pclo = g.lo((s - 1) * STRIP + 1);
+                pdelta = cclo - pclo - sw - 8;
+                pmin = pclo + 8;
+            }
         }
-        int64_t idx = (int64_t)s * sw + (j - cclo);
+        // word indices fit 32 bits: a slot holds at most 4,096 strips of
+        // 32,767 columns
+        const int idx = s * sw + (j - cclo);
         uint32_t w;
         if (idx == ck) {
             w = cw;
         } else if (idx == nk) {
             w = nw;
         } else {
-            w = tb[(size_t)idx * TBS];
+            w = tb[(size_t)(uint32_t)idx * TBS];
         }
         ck = idx;
         cw = w;
         if (j - 1 >= cclo) {  // prefetch the word one column left (same strip)
             nk = idx - 1;
-            nw = tb[(size_t)nk * TBS];
+            nw = tb[(size_t)(uint32_t)nk * TBS];
         } else {
             nk = -1;
         }
@@ -428,16 +436,9 @@ struct Walker {
         // global traceback of the thread kernels): the walk mostly runs
         // along the diagonal, and the lines it reads have left L2 since the
         // fill wrote them
-        if (TBS == 32) {
-            const int pi = i - 8, pj = j - 8;
-            if (pi >= 1 && pj >= 1) {
-                const int ps = (pi - 1) >> 3;
-                const int pclo = ps == s ? cclo : g.lo(ps * STRIP + 1);
-                if (pj >= pclo) {
-                    const uint32_t *pa = tb + (size_t)((int64_t)ps * sw + (pj - pclo)) * TBS;
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pa));
-                }
-            }
+        if (TBS == 32 && s > 0 && j >= pmin) {
+            const uint32_t *pa = tb + (size_t)(uint32_t)(idx + pdelta) * TBS;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(pa));
         }
         int sh = 2 * (7 - r);
         uint32_t hsrc = (w >> sh) & 3u;
@@ -449,13 +450,8 @@ struct Walker {
         if (rleft < 0) rfill();
         if (wleft < 0) wfill();
         const uint32_t q = (rnb & 1u) ? 4u : (rv & 3u), rc = (wnb & 1u) ? 4u : (wv & 3u);
-        // diagonal kinds K_MM 0 / K_MX 1 / K_MZ 2 without branches (a match
-        // and an edit-tolerated pair exclude each other)
-        const int mm = (q == rc) & (q < 4u);
-        const int mz = ((K.edit_dir == ESP_EDIT_AG) & (q == 2u) & (rc == 0u)) |
-                       ((K.edit_dir == ESP_EDIT_TC) & (q == 1u) & (rc == 3u));
         const int open = state == 0;
-        const int kdiag = 1 - mm + mz;
+        const int kdiag = (int)((K.dkind >> (2 * (q * 5 + rc))) & 3u);
         const int kvert = open ? K_IO : K_IE, khor = open ? K_DO : K_DE;
         kind = eff == 2u ? kdiag : (eff == 1u ? kvert : khor);
         state = eff == 2u ? 0 : (eff == 1u ? (eo ? 0 : 1) : (fo ? 0 : 2));
@@ -491,16 +487,16 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
     int pst[REC_WORDS], bmx[REC_WORDS];
     // walk 1: number of steps N, total T, trail (with the prefix sum before
     // step `trail` and the cell the walk stood on there)
-    int N = 0, P = 0, trail = 0, ptrail = 0, tr_i = F.best_i, tr_j = F.best_j;
+    int N = 0, P = 0, trail = 0;
     {
         Walker<TBS> W(g, tb, sw, read, win, K, F.best_i, F.best_j);
         int kind;
-        uint32_t acc = 0;
+        uint32_t acc = 0;  // the open block's kinds, entering at the top
         int bm = INT_MIN, pb = 0;
         while (W.step(kind)) {
             P += dtab[kind];
             bm = max(bm, P);
-            acc |= (uint32_t)kind << (4 * (N & 7));
+            acc = (acc >> 4) | ((uint32_t)kind << 28);
             N++;
             if ((N & 7) == 0) {
                 if ((N >> 3) <= REC_WORDS) {
@@ -508,19 +504,13 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
                     pst[(N >> 3) - 1] = pb;
                     bmx[(N >> 3) - 1] = bm;
                 }
-                acc = 0;
                 bm = INT_MIN;
                 pb = P;
             }
-            if (P <= 0) {
-                trail = N;
-                ptrail = P;
-                tr_i = W.i;
-                tr_j = W.j;
-            }
+            if (P <= 0) trail = N;
         }
         if ((N & 7) && (N >> 3) < REC_WORDS) {
-            rec[N >> 3] = acc;
+            rec[N >> 3] = acc >> (4 * (8 - (N & 7)));
             pst[N >> 3] = pb;
             bmx[N >> 3] = bm;
         }
@@ -602,6 +592,16 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
             emit((1u << 4) | (uint32_t)op);
             first_op = last_op = op;
         } else {
+            // the cell the walk stood on before step `trail` and the prefix
+            // sum there, from the record
+            int tr_i = F.best_i, tr_j = F.best_j, ptrail = 0;
+            for (int t = 0; t < trail; t++) {
+                const int kind = (int)((rec[t >> 3] >> (4 * (t & 7))) & 15u);
+                const int op = kind_op(kind);
+                ptrail += dtab[kind];
+                if (op != ESP_OP_D) tr_i--;
+                if (op != ESP_OP_I) tr_j--;
+            }
             // runs of steps [trail, ue] in walk order; the kept region ends
             // (forward order) where the walk stood before step `trail`
             read_end = (uint32_t)tr_i;
@@ -1584,6 +1584,17 @@ int make_gotoh_const(const esp_extend_params &p, GotohConst &k) {
     int smax = 0;
     for (int i = 0; i < 25; i++) smax = lut[i] > smax ? lut[i] : smax;
     k.max_m = smax > 0 ? 8191 / smax : 32767;
+    // traceback kind of a diagonal step by read code * 5 + window code:
+    // K_MM for equal ACGT codes, K_MZ for the edit-tolerated pair, K_MX
+    // otherwise (a match and a tolerated pair exclude each other)
+    k.dkind = 0;
+    for (int q = 0; q < 5; q++)
+        for (int c = 0; c < 5; c++) {
+            const bool mz = (p.edit_dir == ESP_EDIT_AG && q == 2 && c == 0) ||
+                            (p.edit_dir == ESP_EDIT_TC && q == 1 && c == 3);
+            const int kd = (q == c && q < 4) ? K_MM : (mz ? K_MZ : K_MX);
+            k.dkind |= (uint64_t)kd << (2 * (q * 5 + c));
+        }
     for (int rc = 0; rc < 5; rc++) {
         uint32_t w[2] = {0, 0};
         for (int fc = 0; fc < 8; fc++) {
