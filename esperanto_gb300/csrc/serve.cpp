@@ -220,7 +220,7 @@ void copy_out(Slot &sl) {
 }
 
 // Publish a request as done (server lock held).
-void complete(esp_server *s, Request *r, int32_t status) {
+void complete(Request *r, int32_t status) {
     r->status = status;
     r->latency_ms =
         std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count();
@@ -261,7 +261,7 @@ void worker_loop(esp_server *s) {
                 s->sched.finish(sl.L, finished);
                 for (serve::Job *j : finished) {
                     Request *r = (Request *)j->user;
-                    complete(s, r, r->err);
+                    complete(r, r->err);
                 }
                 sl.busy = false;
             }
@@ -269,7 +269,7 @@ void worker_loop(esp_server *s) {
             if (s->closing) {  // requests none of whose reads started: ESP_ECLOSED
                 finished.clear();
                 s->sched.drop_unstarted(finished);
-                for (serve::Job *j : finished) complete(s, (Request *)j->user, ESP_ECLOSED);
+                for (serve::Job *j : finished) complete((Request *)j->user, ESP_ECLOSED);
                 notify |= !finished.empty();
             }
             if (notify) s->cv_done.notify_all();
@@ -422,7 +422,7 @@ int esp_server_submit(esp_server *s, const esp_serve_request *req, uint64_t *tic
     r->t_submit = Clock::now();
     s->all[r->ticket] = r;
     if (j.n == 0) {
-        complete(s, r, ESP_OK);
+        complete(r, ESP_OK);
     } else {
         s->sched.push(&j);
         s->cv_work.notify_one();
