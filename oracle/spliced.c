@@ -99,8 +99,8 @@ int orc_align_spliced_exons(const orc_contig *c, const uint8_t *read, uint32_t m
     uint64_t total = 0;
     for (uint32_t e = 0; e < n_exons; e++) total += exons[2 * e + 1] - exons[2 * e];
     uint8_t *pseudo = (uint8_t *)malloc(total ? total : 1);
-    uint32_t *bounds = (uint32_t *)malloc(sizeof(uint32_t) * 3 * (n_exons ? n_exons : 1));
-    uint32_t *jl = (uint32_t *)malloc(sizeof(uint32_t) * (n_exons ? n_exons : 1));
+    uint32_t *bounds = (uint32_t *)calloc(3 * (size_t)(n_exons ? n_exons : 1), sizeof(uint32_t));
+    uint32_t *jl = (uint32_t *)calloc(n_exons ? n_exons : 1, sizeof(uint32_t));
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (2 * (m + total) + 8));
     if (!pseudo || !bounds || !jl || !tmp) {
         free(pseudo), free(bounds), free(jl), free(tmp);

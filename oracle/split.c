@@ -146,6 +146,8 @@ int orc_retry_tail_start(const orc_contig *c, const uint8_t *read, uint32_t read
     int32_t lib_bonus = (int32_t)((support < 10 ? support : 10) * 5);
     uint32_t cap = 2 * read_len + 8;
     orc_ext le, re;
+    memset(&le, 0, sizeof(le));  /* a failed first allocation leaves re unset */
+    memset(&re, 0, sizeof(re));
     uint8_t *win = (uint8_t *)malloc((size_t)read_len + 2 * TAIL_MARGIN + 8);
     if (!ext_alloc(&le, cap) || !ext_alloc(&re, cap) || !win) {
         free(le.ops); free(re.ops); free(win);
@@ -184,6 +186,9 @@ int orc_retry_tail_start(const orc_contig *c, const uint8_t *read, uint32_t read
             out->total = total;
             out->left = le;
             out->right = re;
+            /* the buffers now belong to out: forget them before reallocating */
+            memset(&le, 0, sizeof(le));
+            memset(&re, 0, sizeof(re));
             if (!ext_alloc(&le, cap) || !ext_alloc(&re, cap)) {
                 rc = ORC_ENOMEM;
                 break;
