@@ -23,7 +23,7 @@ import numpy as np
 from . import _native as N
 from . import batch as B
 from .extend import ExtendParams
-from .split import CONTIG_DTYPE, Genome
+from .split import Genome
 
 SERVE_READ_DTYPE = np.dtype([("read_pos", "<u8"), ("read_len", "<u4"), ("contig", "<u4"),
                              ("win_start", "<u4"), ("win_len", "<u4"), ("hint_offset", "<i4"),

@@ -1,8 +1,6 @@
 """Shared GPU-vs-oracle comparison helpers."""
 import functools
 
-import numpy as np
-
 import oracle as O
 from esperanto_gb300 import batch as B
 from esperanto_gb300.extend import ExtendParams
