@@ -672,6 +672,19 @@ def reduce_over_ranks(ms, cells, e2e_s, e2e_cells, world, device="cpu"):
     return float(t[0]), float(c[0]), float(t[1]), float(c[1])
 
 
+def repo_libraries():
+    """Shared libraries of this repository mapped into the process (paths
+    relative to the repository), or None where /proc is unavailable."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")}
+    except OSError:
+        return None
+    root = os.path.realpath(ROOT)
+    return sorted(os.path.relpath(p, root) for p in paths
+                  if os.path.realpath(p).startswith(root + os.sep))
+
+
 def reference_arm(args, wl, seed, threads, n_pairs):
     run, sample = wl.cpu_reference(seed, args.cpu_sample, threads)
     for _ in range(args.warmup):
@@ -690,7 +703,10 @@ def reference_arm(args, wl, seed, threads, n_pairs):
             "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            # evidence that the arm ran the oracle port alone: no library of
+            # the GPU path (or of the benchmark tooling) is mapped
+            "repo_libraries_loaded": repo_libraries()}
     print(json.dumps(line), flush=True)
 
 

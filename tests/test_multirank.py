@@ -71,3 +71,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+    # the arm maps the oracle's library only, never the GPU path's
+    libs = d["repo_libraries_loaded"]
+    if libs is not None:
+        assert libs and all(x.startswith("oracle" + os.sep) for x in libs), libs
