@@ -1360,10 +1360,14 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
     const uint32_t oe1 = (uint32_t)(K.oe1 & 0xffff) * 0x10001u;
     const uint32_t oe4 = (uint32_t)(K.oe4 & 0xffff) * 0x10001u;
     const uint32_t ex4 = (uint32_t)(K.ex4 & 0xffff) * 0x10001u;
-    FA.bestHp = FB.bestHp = 2;
-    FA.best_i = FA.best_j = FB.best_i = FB.best_j = 0;
-    FA.trow = FB.trow = 0;
-    FA.tleft = FA.tclamp = FB.tleft = FB.tclamp = false;
+    // the best cell so far of both pairs, packed like the row maxima: its
+    // scaled H, row and column (pair A low half, B high half); the first
+    // touching row of each pair with its left / clamped flags, and bit 15 of
+    // each half of open_halves while that pair has none (all in registers:
+    // FA and FB are the caller's memory)
+    uint32_t bestHp2 = 0x00020002u, bestI2 = 0u, bestJ2 = 0u;
+    uint32_t trow2 = 0u, tflags = 0u;  // touch rows (halves); left / clamped bits 0-1 (A), 2-3 (B)
+    uint32_t open_halves = 0x80008000u;
     int nstrips = (m + STRIP - 1) / STRIP;
     int plo = g.lo(1), phi = g.hi(min(STRIP, m));
     for (int k = 0; k <= phi - plo; k++) rb[(size_t)k * 32] = make_uint2(0x00020002u, NEG2);
@@ -1414,32 +1418,60 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
         if (c_beg <= chi)
             dp_cols2<1, true>(S, oe1, oe4, ex4, c_beg, chi, diag, warena, wposA, wposB, rb, plo, phi, lo7,
                               ta + (size_t)(c_beg - clo) * 32, tbq + (size_t)(c_beg - clo) * 32);
-        // row bookkeeping in row order (extend.rs:795-827), per lane
+        // row bookkeeping in row order (extend.rs:795-827).  The best cell:
+        // a strictly larger row maximum replaces it, both pairs at once with
+        // the keep mask of the row maximum (row_max2)
 #pragma unroll
         for (int r = 0; r < STRIP; r++) {
             if (r < nact) {
-                const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
+                const uint32_t keep = prmt(bestHp2 + 0x80008000u - S.rmax[r], 0u, 0xBB99u);
+                bestHp2 = (bestHp2 & keep) | (S.rmax[r] & ~keep);
+                bestI2 = (bestI2 & keep) | ((uint32_t)(i0 + r) * 0x10001u & ~keep);
+                bestJ2 = (bestJ2 & keep) | (S.arg[r] & ~keep);
+            }
+        }
+        // the first touching row, per pair, until both pairs have one.  A
+        // touch needs a zero half in arg ^ lo (left edge) or, when hi < n, in
+        // rmax ^ Hl (right edge); (x - 0x10001) & ~x has bit 15 of a half set
+        // for every zero half (and may set it in the half above one), so a
+        // strip whose rows have none for a pair still without a touch skips
+        // the exact per-row tests
+        uint32_t zero_halves = 0u;
+        if (open_halves) {
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    FillResult &F = q ? FB : FA;
-                    int rowHp = (int)((S.rmax[r] >> (16 * q)) & 0xffffu);
-                    int argj = (int)((S.arg[r] >> (16 * q)) & 0xffffu);
-                    bool tr = (((S.rmax[r] ^ S.Hl[r]) >> (16 * q)) & 0xffffu) == 0;
-                    if (F.trow == 0) {
-                        if (argj == lo) {
-                            F.trow = i0 + r;
-                            F.tleft = true;
-                            F.tclamp = lo <= 1;
-                        } else if (hi < n && tr) {
-                            F.trow = i0 + r;
-                            F.tleft = false;
-                            F.tclamp = hi >= n;
-                        }
+            for (int r = 0; r < STRIP; r++) {
+                if (r < nact) {
+                    const uint32_t lohi = S.lohi[r];
+                    const uint32_t zl = S.arg[r] ^ ((lohi & 0xffffu) * 0x10001u);
+                    zero_halves |= (zl - 0x00010001u) & ~zl;
+                    if ((int)(lohi >> 16) < n) {
+                        const uint32_t zr = S.rmax[r] ^ S.Hl[r];
+                        zero_halves |= (zr - 0x00010001u) & ~zr;
                     }
-                    if (rowHp > F.bestHp) {
-                        F.bestHp = rowHp;
-                        F.best_i = i0 + r;
-                        F.best_j = argj;
+                }
+            }
+        }
+        if (zero_halves & open_halves) {
+#pragma unroll
+            for (int r = 0; r < STRIP; r++) {
+                if (r < nact) {
+                    const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        const uint32_t bit = 0x8000u << (16 * q);
+                        if (open_halves & bit) {
+                            const int argj = (int)((S.arg[r] >> (16 * q)) & 0xffffu);
+                            const bool tr = (((S.rmax[r] ^ S.Hl[r]) >> (16 * q)) & 0xffffu) == 0;
+                            if (argj == lo) {
+                                trow2 |= (uint32_t)(i0 + r) << (16 * q);
+                                tflags |= (1u | (lo <= 1 ? 2u : 0u)) << (2 * q);
+                                open_halves &= ~bit;
+                            } else if (hi < n && tr) {
+                                trow2 |= (uint32_t)(i0 + r) << (16 * q);
+                                tflags |= (hi >= n ? 2u : 0u) << (2 * q);
+                                open_halves &= ~bit;
+                            }
+                        }
                     }
                 }
             }
@@ -1447,6 +1479,18 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
         plo = lo7;
         phi = (int)(S.lohi[STRIP - 1] >> 16);
     }
+    FA.bestHp = (int)(bestHp2 & 0xffffu);
+    FA.best_i = (int)(bestI2 & 0xffffu);
+    FA.best_j = (int)(bestJ2 & 0xffffu);
+    FB.bestHp = (int)(bestHp2 >> 16);
+    FB.best_i = (int)(bestI2 >> 16);
+    FB.best_j = (int)(bestJ2 >> 16);
+    FA.trow = (int)(trow2 & 0xffffu);
+    FA.tleft = tflags & 1u;
+    FA.tclamp = (tflags >> 1) & 1u;
+    FB.trow = (int)(trow2 >> 16);
+    FB.tleft = (tflags >> 2) & 1u;
+    FB.tclamp = (tflags >> 3) & 1u;
 }
 
 // Out-of-line fill, finish and lone-pair paths of the paired kernel: one
