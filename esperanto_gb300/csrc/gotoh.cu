@@ -1441,10 +1441,10 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
 #pragma unroll
             for (int r = 0; r < STRIP; r++) {
                 if (r < nact) {
-                    const uint32_t lohi = S.lohi[r];
-                    const uint32_t zl = S.arg[r] ^ ((lohi & 0xffffu) * 0x10001u);
+                    const uint32_t lo_r = (uint32_t)g.lo(i0 + r);
+                    const uint32_t zl = S.arg[r] ^ (lo_r * 0x10001u);
                     zero_halves |= (zl - 0x00010001u) & ~zl;
-                    if ((int)(lohi >> 16) < n) {
+                    if (g.hi(i0 + r) < n) {
                         const uint32_t zr = S.rmax[r] ^ S.Hl[r];
                         zero_halves |= (zr - 0x00010001u) & ~zr;
                     }
@@ -1455,7 +1455,7 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
 #pragma unroll
             for (int r = 0; r < STRIP; r++) {
                 if (r < nact) {
-                    const int lo = (int)(S.lohi[r] & 0xffffu), hi = (int)(S.lohi[r] >> 16);
+                    const int lo = g.lo(i0 + r), hi = g.hi(i0 + r);
 #pragma unroll
                     for (int q = 0; q < 2; q++) {
                         const uint32_t bit = 0x8000u << (16 * q);
@@ -1477,7 +1477,7 @@ __device__ void dp_fill2(const GotohConst &K, const uint32_t *__restrict__ s_lut
             }
         }
         plo = lo7;
-        phi = (int)(S.lohi[STRIP - 1] >> 16);
+        phi = g.hi(i0 + STRIP - 1);
     }
     FA.bestHp = (int)(bestHp2 & 0xffffu);
     FA.best_i = (int)(bestI2 & 0xffffu);
