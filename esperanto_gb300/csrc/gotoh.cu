@@ -485,8 +485,8 @@ __device__ void dp_finish(const GotohConst &K, const int8_t *__restrict__ lut, c
     // that the trim below finds its cut by blocks instead of re-walking.
     uint32_t rec[REC_WORDS];
     int pst[REC_WORDS], bmx[REC_WORDS];
-    // walk 1: number of steps N, total T, trail (with the prefix sum before
-    // step `trail` and the cell the walk stood on there)
+    // walk 1: number of steps N, total T and trail (the walk's steps up to
+    // and including its last non-positive prefix sum)
     int N = 0, P = 0, trail = 0;
     {
         Walker<TBS> W(g, tb, sw, read, win, K, F.best_i, F.best_j);
