@@ -295,6 +295,12 @@ __device__ FillResult dp_fill(const GotohConst &K, const uint32_t *__restrict__ 
             dp_cols<0, false, HASN>(S, K, b_beg, b_end, diag, win, rb, plo, phi, lo7,
                                     tbp + (size_t)(b_beg - clo) * 32);
         int c_beg = max(lo7 + 1, hi0);
+        // the row windows again rather than kept live across the interior
+#pragma unroll
+        for (int r = 0; r < STRIP; r++) {
+            S.lo[r] = g.lo(i0 + r);
+            S.hi[r] = g.hi(i0 + r);
+        }
         if (c_beg <= chi)
             dp_cols<1, true, HASN>(S, K, c_beg, chi, diag, win, rb, plo, phi, lo7,
                                    tbp + (size_t)(c_beg - clo) * 32);
