@@ -712,24 +712,33 @@ def reference_arm(args, wl, seed, threads, n_pairs):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4])
-    ap.add_argument("--genome-bases", type=int, default=3_100_000_000)
-    ap.add_argument("--pool", type=int, default=48)
-    ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--gpus", type=int, default=1,
+                    help="GPUs of the node (one rank each under torchrun; replicas)")
+    ap.add_argument("--steps", type=int, default=5, help="timed steps")
+    ap.add_argument("--warmup", type=int, default=3, help="untimed warm-up steps")
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"],
+                    help="reference: the oracle port of the reference on the host cores")
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4],
+                    help="0 banded 150x214, 1 Myers, 2 mixed-length (headline), "
+                         "3 split-read rescue, 4 serve loop")
+    ap.add_argument("--genome-bases", type=int, default=3_100_000_000,
+                    help="resident genome of the serve workload")
+    ap.add_argument("--pool", type=int, default=48, help="serve: distinct requests generated")
+    ap.add_argument("--streams", type=int, default=4, help="serve: launch slots")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="seconds at each of 70%% and 80%% of peak in the serve phase")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the serve phase of the default (mixed-length) line")
     ap.add_argument("--no-others", action="store_true",
                     help="skip the other workloads' measurements in the default line")
-    ap.add_argument("--pairs", type=int, default=0)
-    ap.add_argument("--cpu-sample", type=int, default=16384)
-    ap.add_argument("--e2e-steps", type=int, default=8)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pairs", type=int, default=0,
+                    help="pairs (reads) of the workload; 0 = its full size")
+    ap.add_argument("--cpu-sample", type=int, default=16384,
+                    help="pairs per step of the CPU baseline / reference arm")
+    ap.add_argument("--e2e-steps", type=int, default=8,
+                    help="end-to-end steps through the host API (median reported)")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the oracle-port CPU baseline of the line")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the per-length-class kernel autotuning (profiling runs)")
     args = ap.parse_args()
