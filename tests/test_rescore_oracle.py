@@ -1,7 +1,8 @@
 """Oracle of the strict rescoring walk (align.rs:1060-1165 rescore_with):
-hand-worked known answers from the reference's rules (the reference has no
-direct test of rescore_with), and the kernel's intron-length-penalty table
-against the host's f64 formula (splice.rs:119-121)."""
+pinned to the reference's own rescore_strict tests (align.rs:4215-4303),
+plus hand-worked known answers of its rules (editing directions, N, clips,
+deletions, known and novel introns), and the kernel's intron-length-penalty
+table against the host's f64 formula (splice.rs:119-121)."""
 import pytest
 
 import oracle as O
@@ -54,3 +55,38 @@ def test_intron_penalty_table_matches_f64_formula():
     lens += [int(1.37 ** k) for k in range(20, 71)] + [2 ** 32 - 1]
     for n in lens:
         assert R.intron_length_penalty(n) == O.intron_length_penalty(n), n
+
+
+def test_pinned_to_the_reference_rescore_strict_tests():
+    """align.rs:4215-4303 (rescore_strict_manual_cigars,
+    rescore_strict_splice_signal): rescore_strict is rescore_with with no
+    exempt direction."""
+    f = {k: i for i, k in enumerate(O.STRICT_FIELDS)}
+    ref = O.Contig(b"ACGT" * 50)
+    read = (b"ACGT" * 13)[:50]
+    s = O.rescore(ref, 0, 0, read, [M(50)])
+    assert (s[f["score"]], s[f["matches"]], s[f["mm"]], s[f["aligned"]]) == (100, 50, 0, 50)
+    r2 = bytearray(read)
+    r2[25] = ord("C") if r2[25] == ord("A") else ord("A")
+    s = O.rescore(ref, 0, 0, bytes(r2), [M(50)])
+    assert (s[f["score"]], s[f["mm"]]) == (49 * 2 - 4, 1)
+    r3 = bytearray(read)
+    r3[24] = ord("G")  # ref A at 24 ("ACGT" repeats): an A>G editing-type substitution
+    s = O.rescore(ref, 0, 0, bytes(r3), [M(50)])
+    assert (s[f["score"]], s[f["mm"]]) == (49 * 2 - 4, 0)
+    assert s[f["ea_ag"]] + s[f["ea_tc"]] == 1
+    ins_read = read[:24] + b"TT" + read[24:48]
+    s = O.rescore(ref, 0, 0, ins_read, [M(24), I(2), M(24)])
+    assert (s[f["score"]], s[f["ins"]]) == (48 * 2 - (4 + 2 * 2), 1)
+    # exon1 | GT + 56 N + AG | exon2; the read spans 20 + 20 exon bases
+    exon1 = b"ACGTTGCAAGGCATTACGACCAAGTTACAGGATCCAAGTTGACGTTACAGGCATTAC"
+    intron = b"GT" + b"N" * 56 + b"AG"
+    exon2 = b"CATGGACTTGAACCTTGACGTACATGGACTTGAACCTTGACGTA"
+    seq = exon1 + intron + exon2
+    start, e2 = len(exon1) - 20, len(exon1) + len(intron)
+    sread = seq[start:len(exon1)] + seq[e2:e2 + 20]
+    sc = O.Contig(seq)
+    s = O.rescore(sc, 0, start, sread, [M(20), N(len(intron)), M(20)])
+    expected = (40 * 2 + O.splice_params_default().gt_ag_bonus
+                - O.intron_length_penalty(len(intron)))
+    assert (s[f["score"]], s[f["n_splice"]], s[f["aligned"]]) == (expected, 1, 40)
