@@ -90,3 +90,45 @@ def test_pinned_to_the_reference_rescore_strict_tests():
     expected = (40 * 2 + O.splice_params_default().gt_ag_bonus
                 - O.intron_length_penalty(len(intron)))
     assert (s[f["score"]], s[f["n_splice"]], s[f["aligned"]]) == (expected, 1, 40)
+
+
+def test_extension_and_rescore_agree_like_the_reference_test():
+    """align.rs:2788-2830 (affine_gap_extension_and_common_rescore_agree):
+    over a 160-base xorshift reference with an internal insertion or
+    deletion of 1, 2, 3 or 7 bases at 80 and, for the editing directions, one
+    edit in [15, 40), the full-matrix extension's score equals the strict
+    rescore of its own placement under the same direction."""
+    state, ref = 0x75BCD15, bytearray()
+    for _ in range(160):  # the reference test's generator
+        state ^= (state << 13) & ((1 << 64) - 1)
+        state ^= state >> 7
+        state ^= (state << 17) & ((1 << 64) - 1)
+        ref.append(b"ACGT"[state & 3])
+    ref = bytes(ref)
+    contig = O.Contig(ref)
+    checked = 0
+    for insertion in (False, True):
+        for n in (1, 2, 3, 7):
+            q = bytearray(ref)
+            if insertion:
+                b = next(c for c in b"ACGT" if c != ref[79] and c != ref[80])
+                q[80:80] = bytes([b]) * n
+            else:
+                del q[80:80 + n]
+            for edit in (O.EDIT_OFF, O.EDIT_AG, O.EDIT_TC):
+                e = bytearray(q)
+                if edit != O.EDIT_OFF:
+                    frm, to = (b"A", b"G") if edit == O.EDIT_AG else (b"T", b"C")
+                    k = next(i for i in range(15, 40) if e[i] == frm[0])
+                    e[k] = to[0]
+                ext = O.extend(bytes(e), ref, O.Params(edit_dir=edit))
+                if edit == O.EDIT_OFF:
+                    # the score and gap the reference asserts for this read
+                    # mapped (align.rs:2838-2848)
+                    assert ext.score == (160 - (0 if insertion else n)) * 2 - 4 - 2 * n
+                    assert ("I" if insertion else "D", n) in ext.cigar
+                ops = [(ln << 4) | O.OP_CHARS.index(c) for c, ln in ext.cigar]
+                s = O.rescore(contig, 0, ext.ref_start, bytes(e), ops, edit_dir=edit)
+                assert ext.score == s[0], (insertion, n, edit, ext.cigar)
+                checked += 1
+    assert checked == 24
